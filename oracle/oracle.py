@@ -1,0 +1,208 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference's hot-path arithmetic in plain FP64 C++
+(``ew_oracle.cpp``).  Only the test-suite, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` import this module; the product package never
+does.  ``build()`` compiles the shared library with the Makefile next to it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libew_oracle.so")
+
+INTEGRATORS = {"LSRK45R2": 0, "clRK4": 1, "ADER": 2, "ADERADCONFULL": 3}
+
+_lib = None
+
+
+def build(quiet=True):
+    """Compile the oracle library (idempotent)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        L.ewo_create.restype = P
+        L.ewo_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, dp, i32p, dp, dp]
+        L.ewo_create_hypercube.restype = P
+        L.ewo_create_hypercube.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_int]
+        L.ewo_destroy.argtypes = [P]
+        L.ewo_n_cells.restype = ctypes.c_int64
+        L.ewo_n_cells.argtypes = [P]
+        L.ewo_n_dofs.restype = ctypes.c_int64
+        L.ewo_n_dofs.argtypes = [P]
+        L.ewo_vertices.restype = dp
+        L.ewo_vertices.argtypes = [P]
+        L.ewo_neighbors.restype = i32p
+        L.ewo_neighbors.argtypes = [P]
+        L.ewo_set_ader_post.argtypes = [P, ctypes.c_int]
+        L.ewo_time_step.restype = ctypes.c_double
+        L.ewo_time_step.argtypes = [P, ctypes.c_double]
+        L.ewo_quadrature_points.argtypes = [P, dp]
+        L.ewo_project_reference.argtypes = [P, ctypes.c_int, ctypes.c_double, dp]
+        L.ewo_project_modes.argtypes = [P, ctypes.c_int, dp, ip, ctypes.c_double, dp]
+        L.ewo_apply.argtypes = [P, dp, dp, ctypes.c_double]
+        L.ewo_rk_update.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                    dp, dp, dp]
+        for name in ("ewo_lsrk45_step", "ewo_clrk4_step", "ewo_ader_step",
+                     "ewo_aderadconfull_step", "ewo_ader_taylor", "ewo_apply_ader"):
+            getattr(L, name).argtypes = [P, ctypes.c_double, dp, dp]
+        L.ewo_errors_reference.argtypes = [P, dp, ctypes.c_int, ctypes.c_double, dp]
+        L.ewo_errors_modes.argtypes = [P, dp, ctypes.c_int, dp, ip, ctypes.c_double, dp]
+        L.ewo_run_reference.restype = ctypes.c_int
+        L.ewo_run_reference.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, dp,
+                                        ctypes.c_int, dp]
+        L.ewo_last_error.restype = ctypes.c_char_p
+        L.ewo_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Problem:
+    """An oracle operator over one mesh: the CPU restatement of
+    WaveEquationOperation<dim,k> plus its integrators."""
+
+    def __init__(self, handle, dim, degree):
+        if not handle:
+            raise RuntimeError(lib().ewo_last_error().decode())
+        self.h = handle
+        self.dim = dim
+        self.degree = degree
+        self.n_cells = lib().ewo_n_cells(handle)
+        self.n_dofs = lib().ewo_n_dofs(handle)
+
+    @classmethod
+    def hypercube(cls, dim, degree, n_intervals, n_refinements=0, transform=0.0, boundary_id=2):
+        h = lib().ewo_create_hypercube(dim, degree, n_intervals, n_refinements, transform,
+                                       boundary_id)
+        return cls(h, dim, degree)
+
+    @classmethod
+    def from_mesh(cls, dim, degree, vertices, neighbors, speed, density):
+        vertices = np.ascontiguousarray(vertices, dtype=np.float64)
+        neighbors = np.ascontiguousarray(neighbors, dtype=np.int32)
+        speed = np.ascontiguousarray(speed, dtype=np.float64)
+        density = np.ascontiguousarray(density, dtype=np.float64)
+        n_cells = speed.shape[0]
+        h = lib().ewo_create(dim, degree, n_cells, _dp(vertices),
+                             neighbors.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                             _dp(speed), _dp(density))
+        return cls(h, dim, degree)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ewo_destroy(self.h)
+            self.h = None
+
+    def vertices(self):
+        nv = (1 << self.dim) * self.dim
+        p = lib().ewo_vertices(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.n_cells * nv,)).copy().reshape(
+            self.n_cells, 1 << self.dim, self.dim)
+
+    def neighbors(self):
+        p = lib().ewo_neighbors(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.n_cells * 2 * self.dim,)).copy().reshape(
+            self.n_cells, 2 * self.dim)
+
+    def set_ader_post(self, on):
+        lib().ewo_set_ader_post(self.h, int(bool(on)))
+
+    def time_step(self, cfl_scaled):
+        return lib().ewo_time_step(self.h, cfl_scaled)
+
+    def zeros(self):
+        return np.zeros(self.n_dofs, dtype=np.float64)
+
+    def project_reference(self, modes, t=0.0):
+        u = self.zeros()
+        lib().ewo_project_reference(self.h, modes, t, _dp(u))
+        return u
+
+    def project_modes(self, amps, kvecs, t=0.0):
+        amps = np.ascontiguousarray(amps, dtype=np.float64)
+        kv = np.zeros((len(amps), 3), dtype=np.int32)
+        kv[:, :len(kvecs[0])] = np.asarray(kvecs)
+        u = self.zeros()
+        lib().ewo_project_modes(self.h, len(amps), _dp(amps),
+                                kv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), t, _dp(u))
+        return u
+
+    def apply(self, src, boundary_fac=1.0):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = self.zeros()
+        lib().ewo_apply(self.h, _dp(src), _dp(dst), boundary_fac)
+        return dst
+
+    def lsrk45_step(self, dt, vec_n, vec_np):
+        lib().ewo_lsrk45_step(self.h, dt, _dp(vec_n), _dp(vec_np))
+
+    def clrk4_step(self, dt, vec_n, vec_np):
+        lib().ewo_clrk4_step(self.h, dt, _dp(vec_n), _dp(vec_np))
+
+    def ader_step(self, dt, vec_n, vec_np):
+        lib().ewo_ader_step(self.h, dt, _dp(vec_n), _dp(vec_np))
+
+    def aderadconfull_step(self, dt, vec_n, vec_np):
+        lib().ewo_aderadconfull_step(self.h, dt, _dp(vec_n), _dp(vec_np))
+
+    def ader_taylor(self, dt, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        T = self.zeros()
+        lib().ewo_ader_taylor(self.h, dt, _dp(src), _dp(T))
+        return T
+
+    def apply_ader(self, dt, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = self.zeros()
+        lib().ewo_apply_ader(self.h, dt, _dp(src), _dp(dst))
+        return dst
+
+    def errors_reference(self, u, modes, t):
+        out = np.zeros(3)
+        lib().ewo_errors_reference(self.h, _dp(np.ascontiguousarray(u)), modes, t, _dp(out))
+        return out
+
+    def errors_modes(self, u, amps, kvecs, t):
+        amps = np.ascontiguousarray(amps, dtype=np.float64)
+        kv = np.zeros((len(amps), 3), dtype=np.int32)
+        kv[:, :len(kvecs[0])] = np.asarray(kvecs)
+        out = np.zeros(3)
+        lib().ewo_errors_modes(self.h, _dp(np.ascontiguousarray(u)), len(amps), _dp(amps),
+                               kv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), t, _dp(out))
+        return out
+
+    def run_reference(self, integrator, cfl, final_time, tick, modes, max_time_steps=1000000):
+        rows = np.zeros((4096, 5))
+        dt = np.zeros(1)
+        nr = lib().ewo_run_reference(self.h, INTEGRATORS[integrator], cfl, final_time, tick, modes,
+                                     max_time_steps, _dp(rows), rows.shape[0], _dp(dt))
+        if nr < 0:
+            raise RuntimeError(lib().ewo_last_error().decode())
+        return rows[:nr].copy(), float(dt[0])
+
+
+def num_threads():
+    return lib().ewo_num_threads()
