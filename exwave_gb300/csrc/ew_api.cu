@@ -1,0 +1,873 @@
+// ew_api.cu -- the C ABI (include/exwave_gb300.h): context set-up (mesh
+// validation, flattening of geometry and materials to device arrays), the
+// integrator drivers that sequence the fused kernels, and the small
+// non-hot kernels (projection of initial fields, L2 errors, vector update).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/exwave_gb300.h"
+#include "ew_basis.h"
+#include "ew_launch.h"
+
+namespace ew {
+namespace {
+
+KernelTable g_tables[2][9];
+std::once_flag g_tables_once;
+
+void init_tables() {
+  kernel_table_d2_2(g_tables[0][2]);
+  kernel_table_d2_3(g_tables[0][3]);
+  kernel_table_d2_4(g_tables[0][4]);
+  kernel_table_d2_5(g_tables[0][5]);
+  kernel_table_d2_6(g_tables[0][6]);
+  kernel_table_d2_7(g_tables[0][7]);
+  kernel_table_d2_8(g_tables[0][8]);
+  kernel_table_d3_2(g_tables[1][2]);
+  kernel_table_d3_3(g_tables[1][3]);
+  kernel_table_d3_4(g_tables[1][4]);
+  kernel_table_d3_5(g_tables[1][5]);
+  kernel_table_d3_6(g_tables[1][6]);
+  kernel_table_d3_7(g_tables[1][7]);
+  kernel_table_d3_8(g_tables[1][8]);
+}
+
+thread_local std::string g_create_error;
+
+// LowStorageRK45Reg2 coefficients (time_integrators.cc:243-252)
+constexpr double kA21 = 970286171893. / 4311952581923.;
+constexpr double kA32 = 6584761158862. / 12103376702013.;
+constexpr double kA43 = 2251764453980. / 15575788980749.;
+constexpr double kA54 = 26877169314380. / 34165994151039.;
+constexpr double kB1 = 1153189308089. / 22510343858157.;
+constexpr double kB2 = 1772645290293. / 4653164025191.;
+constexpr double kB3 = -1672844663538. / 4480602732383.;
+constexpr double kB4 = 2114624349019. / 3568978502595.;
+constexpr double kB5 = 5198255086312. / 14908931495163.;
+
+constexpr int kMaxModes = 8;
+struct Modes {
+  int n;
+  double amp[kMaxModes];
+  int k[kMaxModes][3];
+};
+
+// ---------------------------------------------------------------- kernels
+__global__ void rk_update_kernel(int64_t n, double f1, double f2, int is_last, const double* v1,
+                                 double* v2, double* v3) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (is_last) {
+      v2[i] = v3[i] + f1 * v1[i];
+    } else {
+      const double up = v1[i];
+      const double a = v2[i] + f1 * up;
+      v2[i] = a;
+      v3[i] = a + f2 * up;
+    }
+  }
+}
+
+__device__ void map_point_dev(int dim, const double* V, const double* xi, double* x) {
+  const int nv = 1 << dim;
+  for (int i = 0; i < dim; ++i) x[i] = 0.0;
+  for (int v = 0; v < nv; ++v) {
+    double phi = 1.0;
+    for (int e = 0; e < dim; ++e) phi *= ((v >> e) & 1) ? xi[e] : 1.0 - xi[e];
+    for (int i = 0; i < dim; ++i) x[i] += V[v * dim + i] * phi;
+  }
+}
+
+__device__ double jac_det_dev(int dim, const double* V, const double* xi) {
+  const int nv = 1 << dim;
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int v = 0; v < nv; ++v)
+    for (int j = 0; j < dim; ++j) {
+      double dphi = ((v >> j) & 1) ? 1.0 : -1.0;
+      for (int e = 0; e < dim; ++e)
+        if (e != j) dphi *= ((v >> e) & 1) ? xi[e] : 1.0 - xi[e];
+      for (int i = 0; i < dim; ++i) J[i][j] += V[v * dim + i] * dphi;
+    }
+  if (dim == 2) return J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  return J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+}
+
+__device__ void membrane_dev(int dim, const Modes& ms, const double* x, double t, double* out) {
+  const double pi = 3.14159265358979323846;
+  for (int f = 0; f <= dim; ++f) out[f] = 0.0;
+  for (int m = 0; m < ms.n; ++m) {
+    double ksq = 0.0;
+    for (int d = 0; d < dim; ++d) ksq += (double)ms.k[m][d] * ms.k[m][d];
+    const double w = pi * sqrt(ksq);
+    double prod = 1.0;
+    for (int d = 0; d < dim; ++d) prod *= sin(ms.k[m][d] * pi * x[d]);
+    out[dim] += ms.amp[m] * cos(w * t) * prod;
+    for (int c = 0; c < dim; ++c) {
+      double v = -ms.amp[m] * (ms.k[m][c] * pi / w) * sin(w * t);
+      for (int d = 0; d < dim; ++d)
+        v *= (d == c) ? cos(ms.k[m][d] * pi * x[d]) : sin(ms.k[m][d] * pi * x[d]);
+      out[c] += v;
+    }
+  }
+}
+
+// physical coordinates of the Gauss points: one thread per (cell, point)
+__global__ void qpoints_kernel(const double* verts, int64_t n_cells, int dim, int np,
+                               const double* nodes, double* xyz) {
+  int N = 1;
+  for (int d = 0; d < dim; ++d) N *= np;
+  const int64_t total = n_cells * N;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / N;
+    int q = (int)(idx - c * N);
+    double xi[3] = {0, 0, 0};
+    for (int e = 0; e < dim; ++e) {
+      xi[e] = nodes[q % np];
+      q /= np;
+    }
+    map_point_dev(dim, verts + c * (1 << dim) * dim, xi, xyz + idx * dim);
+  }
+}
+
+__global__ void project_membrane_kernel(const double* verts, int64_t n_cells, int dim, int np,
+                                        const double* nodes, Modes ms, double t, double* u) {
+  int N = 1;
+  for (int d = 0; d < dim; ++d) N *= np;
+  const int F = dim + 1;
+  const int64_t total = n_cells * N;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / N;
+    const int q0 = (int)(idx - c * N);
+    int q = q0;
+    double xi[3] = {0, 0, 0}, x[3] = {0, 0, 0}, ex[4];
+    for (int e = 0; e < dim; ++e) {
+      xi[e] = nodes[q % np];
+      q /= np;
+    }
+    map_point_dev(dim, verts + c * (1 << dim) * dim, xi, x);
+    membrane_dev(dim, ms, x, t, ex);
+    for (int f = 0; f < F; ++f) u[c * F * N + f * N + q0] = ex[f];
+  }
+}
+
+__global__ void project_gaussian_kernel(const double* verts, int64_t n_cells, int dim, int np,
+                                        const double* nodes, double x0, double x1, double x2,
+                                        double width, double amp, double* u) {
+  int N = 1;
+  for (int d = 0; d < dim; ++d) N *= np;
+  const int F = dim + 1;
+  const int64_t total = n_cells * N;
+  const double c0[3] = {x0, x1, x2};
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / N;
+    const int q0 = (int)(idx - c * N);
+    int q = q0;
+    double xi[3] = {0, 0, 0}, x[3] = {0, 0, 0};
+    for (int e = 0; e < dim; ++e) {
+      xi[e] = nodes[q % np];
+      q /= np;
+    }
+    map_point_dev(dim, verts + c * (1 << dim) * dim, xi, x);
+    double r2 = 0.0;
+    for (int e = 0; e < dim; ++e) r2 += (x[e] - c0[e]) * (x[e] - c0[e]);
+    for (int f = 0; f < dim; ++f) u[c * F * N + f * N + q0] = 0.0;
+    u[c * F * N + dim * N + q0] = amp * exp(-r2 / (2.0 * width * width));
+  }
+}
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) s += red[i];
+  return s;
+}
+
+// L2 norms with QGauss(k+2): values interpolated from the k+1 Gauss points
+// (interp[m][np]), exact solution given by `ms` (mode 0) or a second state
+// (mode 1: difference a - b).  acc[0..2] += per-block sums.
+__global__ void l2_kernel(const double* verts, int64_t n_cells, int dim, int np, int m,
+                          const double* interp, const double* qx, const double* qw, const double* a,
+                          const double* b, Modes ms, double t, int mode, double* acc) {
+  __shared__ double red[32];
+  int N = 1, M = 1;
+  for (int d = 0; d < dim; ++d) {
+    N *= np;
+    M *= m;
+  }
+  const int F = dim + 1;
+  const int64_t total = n_cells * M;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx / M;
+    int p = (int)(idx - c * M);
+    int ia[3] = {0, 0, 0};
+    double xi[3] = {0, 0, 0}, w = 1.0;
+    for (int e = 0; e < dim; ++e) {
+      ia[e] = p % m;
+      p /= m;
+      xi[e] = qx[ia[e]];
+      w *= qw[ia[e]];
+    }
+    double va[4] = {0, 0, 0, 0}, vb[4] = {0, 0, 0, 0};
+    for (int q = 0; q < N; ++q) {
+      int qq = q;
+      double wgt = 1.0;
+      for (int e = 0; e < dim; ++e) {
+        wgt *= interp[ia[e] * np + qq % np];
+        qq /= np;
+      }
+      for (int f = 0; f < F; ++f) {
+        va[f] += wgt * a[c * F * N + f * N + q];
+        if (mode == 1) vb[f] += wgt * b[c * F * N + f * N + q];
+      }
+    }
+    const double* V = verts + c * (1 << dim) * dim;
+    const double jxw = fabs(jac_det_dev(dim, V, xi)) * w;
+    if (mode == 0) {
+      double x[3] = {0, 0, 0};
+      map_point_dev(dim, V, xi, x);
+      membrane_dev(dim, ms, x, t, vb);
+    }
+    const double dp = va[dim] - vb[dim];
+    s0 += dp * dp * jxw;
+    for (int d = 0; d < dim; ++d) {
+      const double dv = va[d] - vb[d];
+      s1 += dv * dv * jxw;
+    }
+    s2 += vb[dim] * vb[dim] * jxw;
+  }
+  const double r0 = block_sum(s0, red);
+  const double r1 = block_sum(s1, red);
+  const double r2 = block_sum(s2, red);
+  if (threadIdx.x == 0) {
+    atomicAdd(acc, r0);
+    atomicAdd(acc + 1, r1);
+    atomicAdd(acc + 2, r2);
+  }
+}
+
+int grid_for(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 1 << 20);
+}
+
+}  // namespace
+}  // namespace ew
+
+// ================================================================ context
+struct ew_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int dim = 0, degree = 0, np = 0, N = 0, F = 0;
+  int64_t n_cells = 0, n_dofs = 0;
+  bool mixed = false, cart = false, post = false;
+  int cb_stage = 1, cb_ck = 1;
+  const ew::KernelTable* kt = nullptr;
+  int32_t* d_nbr = nullptr;
+  void* d_geo = nullptr;
+  void* d_mat = nullptr;
+  double* d_verts = nullptr;
+  void* d_basis = nullptr;
+  double* d_nodes = nullptr;
+  ew::WorkItem* d_work_stage = nullptr;
+  int n_work_stage = 0;
+  ew::WorkItem* d_work_ck = nullptr;
+  int n_work_ck = 0;
+  int grid_stage[ew::N_STAGE_VARIANTS] = {0, 0, 0};
+  int grid_ck = 0;
+  int* d_err = nullptr;
+  double* d_tmp64 = nullptr;
+  float* d_x32[2] = {nullptr, nullptr};
+  double* d_acc = nullptr;
+  double* d_l2 = nullptr;  // interp (m x np), qx (m), qw (m)
+  int l2_m = 0;
+  std::string last_error;
+  int64_t launches = 0;
+};
+
+namespace {
+
+int fail(ew_ctx* c, int code, const std::string& msg) {
+  if (c)
+    c->last_error = msg;
+  else
+    ew::g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(ew_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, EW_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+int dev_alloc(ew_ctx* c, T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(c, EW_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  return EW_OK;
+}
+
+int upload(ew_ctx* c, void* dst, const void* src, size_t bytes) {
+  cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpy");
+  return EW_OK;
+}
+
+void free_ctx(ew_ctx* c) {
+  if (!c) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(c->device);
+  void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
+                  c->d_work_stage, c->d_work_ck, c->d_err, c->d_tmp64, c->d_x32[0],
+                  c->d_x32[1], c->d_acc, c->d_l2};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  cudaSetDevice(prev);
+  delete c;
+}
+
+// Checks of the mesh description (the reference relies on deal.II's
+// Triangulation for these invariants).
+int validate_mesh(const ew_mesh_desc* m, bool* cartesian) {
+  if (!m) return fail(nullptr, EW_ERR_INVALID, "mesh is NULL");
+  if (m->dim != 2 && m->dim != 3) return fail(nullptr, EW_ERR_INVALID, "dim must be 2 or 3");
+  if (m->degree < 1 || m->degree > EW_MAX_DEGREE)
+    return fail(nullptr, m->degree > EW_MAX_DEGREE && m->degree <= 12 ? EW_ERR_UNSUPPORTED
+                                                                      : EW_ERR_INVALID,
+                "degree must be in 1.." + std::to_string(EW_MAX_DEGREE));
+  if (m->n_cells < 1 || m->n_cells > (int64_t)0x7fffffff)
+    return fail(nullptr, EW_ERR_INVALID, "n_cells out of range");
+  if (!m->vertices || !m->neighbors || !m->speed || !m->density)
+    return fail(nullptr, EW_ERR_INVALID, "mesh arrays must not be NULL");
+  const int dim = m->dim, nv = 1 << dim, nf = 2 * dim;
+  bool cart = true;
+  for (int64_t c = 0; c < m->n_cells; ++c) {
+    if (!(m->speed[c] > 0.0) || !(m->density[c] > 0.0) || !std::isfinite(m->speed[c]) ||
+        !std::isfinite(m->density[c]))
+      return fail(nullptr, EW_ERR_INVALID, "speed and density must be positive, cell " +
+                                               std::to_string(c));
+    const double* V = m->vertices + (size_t)c * nv * dim;
+    double scale = 0.0;
+    for (int e = 0; e < dim; ++e) scale = std::max(scale, std::fabs(V[(nv - 1) * dim + e] - V[e]));
+    if (!(scale > 0.0)) return fail(nullptr, EW_ERR_INVALID, "degenerate cell " + std::to_string(c));
+    for (int v = 0; v < nv && cart; ++v)
+      for (int e = 0; e < dim; ++e) {
+        const double ref = ((v >> e) & 1) ? V[(nv - 1) * dim + e] : V[e];
+        if (V[v * dim + e] != ref) cart = false;
+      }
+    for (int f = 0; f < nf; ++f) {
+      const int32_t nb = m->neighbors[c * nf + f];
+      if (nb < 0) {
+        if (nb < -3)
+          return fail(nullptr, EW_ERR_INVALID,
+                      "boundary id must be 1, 2 or 3 (cell " + std::to_string(c) + ")");
+        continue;
+      }
+      if (nb >= m->n_cells)
+        return fail(nullptr, EW_ERR_INVALID, "neighbor index out of range, cell " + std::to_string(c));
+      if (m->neighbors[(int64_t)nb * nf + (f ^ 1)] != (int32_t)c)
+        return fail(nullptr, EW_ERR_INVALID,
+                    "neighbor relation not symmetric at cell " + std::to_string(c));
+      // the shared face must have the same vertices in the same tangential order
+      const int e = f / 2, s = f % 2;
+      const double* W = m->vertices + (size_t)nb * nv * dim;
+      for (int v = 0; v < nv; ++v) {
+        if (((v >> e) & 1) != s) continue;
+        const int w = v ^ (1 << e);
+        for (int d = 0; d < dim; ++d)
+          if (std::fabs(V[v * dim + d] - W[w * dim + d]) > 1e-10 * scale)
+            return fail(nullptr, EW_ERR_INVALID,
+                        "face of cell " + std::to_string(c) +
+                            " does not match its neighbor in standard orientation");
+      }
+    }
+  }
+  *cartesian = cart;
+  return EW_OK;
+}
+
+template <typename Real>
+std::vector<Real> to_real_vec(const std::vector<double>& v) {
+  return std::vector<Real>(v.begin(), v.end());
+}
+
+int build_work(ew_ctx* c, int cb, ew::WorkItem** d_work, int* n_work) {
+  std::vector<ew::WorkItem> w;
+  for (int64_t b = 0; b < c->n_cells; b += cb) {
+    ew::WorkItem it;
+    it.solve = 0;
+    it.cell_begin = (int32_t)b;
+    it.n_cells = (int32_t)std::min<int64_t>(cb, c->n_cells - b);
+    it.pad = 0;
+    w.push_back(it);
+  }
+  int rc = dev_alloc(c, d_work, w.size());
+  if (rc) return rc;
+  *n_work = (int)w.size();
+  return upload(c, *d_work, w.data(), w.size() * sizeof(ew::WorkItem));
+}
+
+int default_cb(int points, int requested) {
+  if (requested > 0) return std::max(1, std::min(requested, 512 / points));
+  return std::max(1, 512 / points);
+}
+
+int check(ew_ctx* c) {
+  if (!c) return EW_ERR_INVALID;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  return EW_OK;
+}
+
+ew::LaunchArgs base_args(ew_ctx* c, bool ck) {
+  ew::LaunchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.single.nbr = c->d_nbr;
+  a.single.geo = c->d_geo;
+  a.single.mat = c->d_mat;
+  a.single.n_cells = c->n_cells;
+  a.single.bf = 1.0f;
+  a.solves = nullptr;
+  a.work = ck ? c->d_work_ck : c->d_work_stage;
+  a.n_work = ck ? c->n_work_ck : c->n_work_stage;
+  a.cells_per_block = ck ? c->cb_ck : c->cb_stage;
+  a.basis = c->d_basis;
+  a.err = c->d_err;
+  return a;
+}
+
+void split(double v, float* hi, float* lo) {
+  *hi = (float)v;
+  *lo = (float)(v - (double)*hi);
+}
+
+int launch_stage(ew_ctx* c, int variant, const double* A, const void* X, void* Xout, double* Aout,
+                 int mode, double f1, double f2, float bf) {
+  ew::LaunchArgs a = base_args(c, false);
+  a.single.X = X;
+  a.single.A = A;
+  a.single.Xout = Xout;
+  a.single.Aout = Aout;
+  a.single.f1 = f1;
+  a.single.f2 = f2;
+  a.single.f1f = (float)f1;
+  split(f1, &a.single.f1_hi, &a.single.f1_lo);
+  split(f1 + f2, &a.single.fb_hi, &a.single.fb_lo);
+  a.single.bf = bf;
+  a.single.mode = mode;
+  const ew::KernelEntry& k = c->kt->stage[variant][c->cart ? 1 : 0];
+  cudaError_t e = k.launch(a, c->grid_stage[variant], c->stream);
+  ++c->launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "stage kernel launch");
+  return EW_OK;
+}
+
+int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
+  ew::LaunchArgs a = base_args(c, true);
+  a.single.X = src;
+  a.single.Xout = T;
+  a.dt = dt;
+  const ew::KernelEntry& k = c->kt->ck[c->mixed ? 1 : 0][c->cart ? 1 : 0][c->post ? 1 : 0];
+  cudaError_t e = k.launch(a, c->grid_ck, c->stream);
+  ++c->launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "ck kernel launch");
+  return EW_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+const char* ew_last_error(const ew_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : ew::g_create_error.c_str();
+}
+
+int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out) {
+  if (!out) return fail(nullptr, EW_ERR_INVALID, "ctx output pointer is NULL");
+  *out = nullptr;
+  std::call_once(ew::g_tables_once, ew::init_tables);
+  bool cart = false;
+  int rc = validate_mesh(mesh, &cart);
+  if (rc) return rc;
+  ew_options opt;
+  std::memset(&opt, 0, sizeof(opt));
+  opt.spectral_evaluation = 1;
+  if (options) opt = *options;
+  if (opt.precision != EW_PREC_FP64 && opt.precision != EW_PREC_MIXED)
+    return fail(nullptr, EW_ERR_INVALID, "precision must be EW_PREC_FP64 or EW_PREC_MIXED");
+  if (!opt.spectral_evaluation)
+    return fail(nullptr, EW_ERR_UNSUPPORTED,
+                "ADER with spectral_evaluation = false is not built (only the spectral "
+                "Cauchy-Kovalevskaya procedure)");
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0)
+    return fail(nullptr, EW_ERR_CUDA, "no CUDA device available");
+  if (opt.device < 0 || opt.device >= ndev) return fail(nullptr, EW_ERR_INVALID, "bad device");
+
+  ew_ctx* c = new ew_ctx;
+  c->device = opt.device;
+  ce = cudaSetDevice(c->device);
+  if (ce != cudaSuccess) {
+    delete c;
+    return fail(nullptr, EW_ERR_CUDA, "cudaSetDevice failed");
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  c->dim = mesh->dim;
+  c->degree = mesh->degree;
+  c->np = mesh->degree + 1;
+  c->F = c->dim + 1;
+  c->N = 1;
+  for (int d = 0; d < c->dim; ++d) c->N *= c->np;
+  c->n_cells = mesh->n_cells;
+  c->n_dofs = c->n_cells * c->F * c->N;
+  c->mixed = opt.precision == EW_PREC_MIXED;
+  c->cart = cart;
+  c->post = opt.use_ader_post != 0;
+  c->kt = &ew::g_tables[c->dim - 2][c->np];
+  const int dim = c->dim, nv = 1 << dim;
+
+  auto bail = [&](int code) {
+    ew::g_create_error = c->last_error;
+    free_ctx(c);
+    return code;
+  };
+
+  // geometry: Cartesian cells keep their extents, others their vertices
+  const int geo_per_cell = cart ? dim : nv * dim;
+  std::vector<double> geo((size_t)c->n_cells * geo_per_cell);
+  for (int64_t i = 0; i < c->n_cells; ++i) {
+    const double* V = mesh->vertices + (size_t)i * nv * dim;
+    if (cart)
+      for (int e = 0; e < dim; ++e) geo[i * dim + e] = V[(nv - 1) * dim + e] - V[e];
+    else
+      std::copy(V, V + nv * dim, geo.begin() + i * nv * dim);
+  }
+  std::vector<double> mat((size_t)c->n_cells * 2);
+  for (int64_t i = 0; i < c->n_cells; ++i) {
+    mat[2 * i] = mesh->density[i];
+    mat[2 * i + 1] = mesh->speed[i];
+  }
+  std::vector<double> basis = ew::basis_table(c->np);
+  const size_t rsz = c->mixed ? sizeof(float) : sizeof(double);
+  if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_geo), geo.size() * rsz)) ||
+      (rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_mat), mat.size() * rsz)) ||
+      (rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_basis), basis.size() * rsz)) ||
+      (rc = dev_alloc(c, &c->d_nbr, (size_t)c->n_cells * 2 * dim)) ||
+      (rc = dev_alloc(c, &c->d_verts, (size_t)c->n_cells * nv * dim)) ||
+      (rc = dev_alloc(c, &c->d_nodes, (size_t)c->np)) || (rc = dev_alloc(c, &c->d_err, 4)) ||
+      (rc = dev_alloc(c, &c->d_acc, 4)))
+    return bail(rc);
+  if (c->mixed) {
+    auto g = to_real_vec<float>(geo), m = to_real_vec<float>(mat), b = to_real_vec<float>(basis);
+    if ((rc = upload(c, c->d_geo, g.data(), g.size() * 4)) ||
+        (rc = upload(c, c->d_mat, m.data(), m.size() * 4)) ||
+        (rc = upload(c, c->d_basis, b.data(), b.size() * 4)))
+      return bail(rc);
+  } else {
+    if ((rc = upload(c, c->d_geo, geo.data(), geo.size() * 8)) ||
+        (rc = upload(c, c->d_mat, mat.data(), mat.size() * 8)) ||
+        (rc = upload(c, c->d_basis, basis.data(), basis.size() * 8)))
+      return bail(rc);
+  }
+  if ((rc = upload(c, c->d_nbr, mesh->neighbors, (size_t)c->n_cells * 2 * dim * 4)) ||
+      (rc = upload(c, c->d_verts, mesh->vertices, (size_t)c->n_cells * nv * dim * 8)))
+    return bail(rc);
+  {
+    ew::GaussRule g = ew::gauss_rule(c->np);
+    if ((rc = upload(c, c->d_nodes, g.x.data(), c->np * 8))) return bail(rc);
+    // QGauss(k+2) interpolation data for the L2 errors
+    const int m = c->np + 1;
+    ew::GaussRule ge = ew::gauss_rule(m);
+    std::vector<double> l2(m * c->np + 2 * m);
+    for (int a = 0; a < m; ++a)
+      for (int i = 0; i < c->np; ++i) l2[a * c->np + i] = ew::lagrange(g.x, i, ge.x[a]);
+    std::copy(ge.x.begin(), ge.x.end(), l2.begin() + m * c->np);
+    std::copy(ge.w.begin(), ge.w.end(), l2.begin() + m * c->np + m);
+    c->l2_m = m;
+    if ((rc = dev_alloc(c, &c->d_l2, l2.size())) || (rc = upload(c, c->d_l2, l2.data(), l2.size() * 8)))
+      return bail(rc);
+  }
+  if (cudaMemset(c->d_err, 0, 4 * sizeof(int)) != cudaSuccess)
+    return bail(fail(c, EW_ERR_CUDA, "cudaMemset"));
+
+  // work lists and persistent grid sizes
+  c->cb_stage = default_cb(c->N, opt.cells_per_block);
+  c->cb_ck = c->cb_stage;
+  const int ck_var = c->mixed ? 1 : 0;
+  while (c->cb_ck > 1 &&
+         c->kt->ck[ck_var][cart][c->post].smem(c->cb_ck) > 200 * 1024)
+    --c->cb_ck;
+  if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
+      (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)))
+    return bail(rc);
+  for (int v = 0; v < ew::N_STAGE_VARIANTS; ++v) {
+    const int occ = c->kt->stage[v][cart].occupancy(c->cb_stage);
+    c->grid_stage[v] = std::max(1, std::min(c->n_work_stage, std::max(occ, 1) * c->num_sms));
+  }
+  {
+    const int occ = c->kt->ck[ck_var][cart][c->post].occupancy(c->cb_ck);
+    c->grid_ck = std::max(1, std::min(c->n_work_ck, std::max(occ, 1) * c->num_sms));
+  }
+  // integrator scratch: FP64 third register (also the ADER Taylor state);
+  // mixed: two FP32 stage inputs (the first also holds the ADER Taylor state)
+  if (c->mixed) {
+    if ((rc = dev_alloc(c, &c->d_x32[0], (size_t)c->n_dofs)) ||
+        (rc = dev_alloc(c, &c->d_x32[1], (size_t)c->n_dofs)))
+      return bail(rc);
+  } else {
+    if ((rc = dev_alloc(c, &c->d_tmp64, (size_t)c->n_dofs))) return bail(rc);
+  }
+  ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) return bail(cuda_fail(c, ce, "set-up"));
+  *out = c;
+  return EW_OK;
+}
+
+void ew_destroy(ew_ctx* ctx) { free_ctx(ctx); }
+
+int ew_set_stream(ew_ctx* ctx, void* stream) {
+  if (!ctx) return EW_ERR_INVALID;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return EW_OK;
+}
+
+int64_t ew_n_dofs(const ew_ctx* ctx) { return ctx ? ctx->n_dofs : -1; }
+int64_t ew_n_cells(const ew_ctx* ctx) { return ctx ? ctx->n_cells : -1; }
+int64_t ew_kernel_launches(const ew_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int ew_apply(ew_ctx* ctx, const double* src, double* dst) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!src || !dst || src == dst) return fail(ctx, EW_ERR_INVALID, "ew_apply: src/dst invalid");
+  const int var = ctx->mixed ? ew::STAGE_MIX_IN64 : ew::STAGE_F64;
+  return launch_stage(ctx, var, nullptr, src, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, 1.0f);
+}
+
+int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const double* v1, double* v2,
+                 double* v3) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!v1 || !v2 || !v3) return fail(ctx, EW_ERR_INVALID, "ew_rk_update: NULL vector");
+  ew::rk_update_kernel<<<ew::grid_for(ctx->n_dofs), 256, 0, ctx->stream>>>(ctx->n_dofs, f1, f2,
+                                                                          is_last, v1, v2, v3);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "rk_update launch");
+}
+
+int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step: vec_n and vec_np must be distinct");
+  using namespace ew;
+  const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
+  const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
+                        0.0};
+  if (!ctx->mixed) {
+    // Three FP64 registers N = vec_n, P = vec_np, T = scratch.  The stage
+    // input is read by neighbouring cells, so the new accumulator goes to
+    // the register not read in this stage; the next stage input overwrites
+    // the old accumulator in place (cell-local).
+    double* N = vec_n;
+    double* P = vec_np;
+    double* T = ctx->d_tmp64;
+    struct S {
+      const double* X;
+      const double* A;
+      double* Xo;
+      double* Ao;
+    } st[5] = {{N, N, T, P}, {T, P, P, N}, {P, N, N, T}, {N, T, T, P}, {T, P, nullptr, P}};
+    for (int s = 0; s < 5; ++s) {
+      rc = launch_stage(ctx, STAGE_F64, st[s].A, st[s].X, st[s].Xo, st[s].Ao,
+                        s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+      if (rc) return rc;
+    }
+    return EW_OK;
+  }
+  // mixed: FP64 accumulator in vec_np (in place), FP32 stage inputs ping-pong
+  float* X0 = ctx->d_x32[0];
+  float* X1 = ctx->d_x32[1];
+  rc = launch_stage(ctx, STAGE_MIX_IN64, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0], f2[0], 1.0f);
+  if (rc) return rc;
+  const float* xin[4] = {X0, X1, X0, X1};
+  float* xout[4] = {X1, X0, X1, nullptr};
+  for (int s = 1; s < 5; ++s) {
+    rc = launch_stage(ctx, STAGE_MIX_IN32, vec_np, xin[s - 1], xout[s - 1], vec_np,
+                      s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+    if (rc) return rc;
+  }
+  return EW_OK;
+}
+
+int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!src || !dst || src == dst) return fail(ctx, EW_ERR_INVALID, "ew_apply_ader: src/dst invalid");
+  void* T = ctx->mixed ? static_cast<void*>(ctx->d_x32[0]) : static_cast<void*>(ctx->d_tmp64);
+  if ((rc = launch_ck(ctx, dt, src, T))) return rc;
+  const int var = ctx->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
+  return launch_stage(ctx, var, nullptr, T, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, -1.0f);
+}
+
+int ew_ader_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_ader_step: vec_n and vec_np must be distinct");
+  void* T = ctx->mixed ? static_cast<void*>(ctx->d_x32[0]) : static_cast<void*>(ctx->d_tmp64);
+  if ((rc = launch_ck(ctx, dt, vec_n, T))) return rc;
+  const int var = ctx->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
+  // vec_np = vec_n - (-M^{-1}A(T)) = vec_n + M^{-1}A(T)
+  return launch_stage(ctx, var, vec_n, T, nullptr, vec_np, ew::MODE_RK_LAST, 1.0, 0.0, 1.0f);
+}
+
+int ew_quadrature_points(ew_ctx* ctx, double* xyz) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!xyz) return fail(ctx, EW_ERR_INVALID, "NULL output");
+  ew::qpoints_kernel<<<ew::grid_for(ctx->n_cells * ctx->N), 256, 0, ctx->stream>>>(
+      ctx->d_verts, ctx->n_cells, ctx->dim, ctx->np, ctx->d_nodes, xyz);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "qpoints launch");
+}
+
+static int make_modes(ew_ctx* ctx, int32_t n_modes, const double* amp, const int32_t* kvec,
+                      ew::Modes* ms) {
+  if (n_modes < 0 || n_modes > ew::kMaxModes || (n_modes > 0 && (!amp || !kvec)))
+    return fail(ctx, EW_ERR_INVALID, "membrane modes: 0..8 modes with amplitudes and wave numbers");
+  std::memset(ms, 0, sizeof(*ms));
+  ms->n = n_modes;
+  for (int m = 0; m < n_modes; ++m) {
+    ms->amp[m] = amp[m];
+    bool nz = false;
+    for (int d = 0; d < 3; ++d) {
+      ms->k[m][d] = kvec[3 * m + d];
+      if (d < ctx->dim && kvec[3 * m + d] != 0) nz = true;
+    }
+    if (!nz) return fail(ctx, EW_ERR_INVALID, "membrane mode with zero wave vector");
+  }
+  return EW_OK;
+}
+
+int ew_project_membrane(ew_ctx* ctx, int32_t n_modes, const double* amp, const int32_t* kvec,
+                        double t, double* u) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  ew::Modes ms;
+  if ((rc = make_modes(ctx, n_modes, amp, kvec, &ms))) return rc;
+  if (!u) return fail(ctx, EW_ERR_INVALID, "NULL output");
+  ew::project_membrane_kernel<<<ew::grid_for(ctx->n_cells * ctx->N), 256, 0, ctx->stream>>>(
+      ctx->d_verts, ctx->n_cells, ctx->dim, ctx->np, ctx->d_nodes, ms, t, u);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "project launch");
+}
+
+int ew_project_gaussian(ew_ctx* ctx, const double* x0, double width, double amp, double* u) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!x0 || !u || !(width > 0.0)) return fail(ctx, EW_ERR_INVALID, "gaussian: bad arguments");
+  ew::project_gaussian_kernel<<<ew::grid_for(ctx->n_cells * ctx->N), 256, 0, ctx->stream>>>(
+      ctx->d_verts, ctx->n_cells, ctx->dim, ctx->np, ctx->d_nodes, x0[0], ctx->dim > 1 ? x0[1] : 0.0,
+      ctx->dim > 2 ? x0[2] : 0.0, width, amp, u);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "project launch");
+}
+
+static int run_l2(ew_ctx* ctx, const double* a, const double* b, const ew::Modes& ms, double t,
+                  int mode, double* out) {
+  cudaError_t e = cudaMemsetAsync(ctx->d_acc, 0, 4 * sizeof(double), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
+  const int m = ctx->l2_m;
+  int M = 1;
+  for (int d = 0; d < ctx->dim; ++d) M *= m;
+  const int grid = (int)std::min<int64_t>(ew::grid_for(ctx->n_cells * M), 8 * ctx->num_sms);
+  ew::l2_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_verts, ctx->n_cells, ctx->dim, ctx->np, m,
+                                               ctx->d_l2, ctx->d_l2 + m * ctx->np,
+                                               ctx->d_l2 + m * ctx->np + m, a, b, ms, t, mode,
+                                               ctx->d_acc);
+  ++ctx->launches;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "l2 launch");
+  double h[4];
+  e = cudaMemcpyAsync(h, ctx->d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "l2 readback");
+  out[0] = std::sqrt(h[0]);
+  out[1] = std::sqrt(h[1]);
+  out[2] = std::sqrt(h[2]);
+  return EW_OK;
+}
+
+int ew_l2_errors_membrane(ew_ctx* ctx, const double* u, int32_t n_modes, const double* amp,
+                          const int32_t* kvec, double t, double out[3]) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  ew::Modes ms;
+  if ((rc = make_modes(ctx, n_modes, amp, kvec, &ms))) return rc;
+  if (!u || !out) return fail(ctx, EW_ERR_INVALID, "NULL argument");
+  return run_l2(ctx, u, nullptr, ms, t, 0, out);
+}
+
+int ew_l2_difference(ew_ctx* ctx, const double* a, const double* b, double out[2]) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!a || !b || !out) return fail(ctx, EW_ERR_INVALID, "NULL argument");
+  ew::Modes ms;
+  std::memset(&ms, 0, sizeof(ms));
+  double o3[3];
+  rc = run_l2(ctx, a, b, ms, 0.0, 1, o3);
+  out[0] = o3[0];
+  out[1] = o3[1];
+  return rc;
+}
+
+int ew_synchronize(ew_ctx* ctx) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+  int flags = 0;
+  e = cudaMemcpy(&flags, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "error flag readback");
+  if (flags) {
+    std::string m = "device error flag";
+    if (flags & ew::ERR_BAD_NEIGHBOR) m += ": neighbor index out of range";
+    if (flags & ew::ERR_BAD_BOUNDARY_ID) m += ": invalid boundary id";
+    if (flags & ew::ERR_BAD_LAUNCH) m += ": launch shape mismatch";
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    return fail(ctx, EW_ERR_DEVICE, m);
+  }
+  return EW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// ew_inst.cu -- instantiates the kernels for one (dimension, points per
+// direction) pair, selected by -DEW_DIM and -DEW_NP, and exports their
+// launchers through a table (one object file per pair, compiled in parallel).
+#include "ew_kernels.cuh"
+#include "ew_launch.h"
+
+#ifndef EW_DIM
+#error "EW_DIM must be defined"
+#endif
+#ifndef EW_NP
+#error "EW_NP must be defined"
+#endif
+
+namespace ew {
+namespace {
+
+constexpr int DIM = EW_DIM;
+constexpr int NP = EW_NP;
+constexpr int N = ipow_c(NP, DIM);
+
+template <typename Kern>
+cudaError_t run(Kern kern, const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<grid, block, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename Kern>
+int blocks_per_sm(Kern kern, int block, size_t smem) {
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+template <typename Real, typename InT, typename OutT, bool CART>
+struct StageK {
+  static size_t smem(int cb) { return (size_t)OpSmem<DIM, NP, CART>(cb).end * sizeof(Real); }
+  static cudaError_t launch(const LaunchArgs& a, int grid, cudaStream_t st) {
+    const int cb = a.cells_per_block;
+    return run(stage_kernel<DIM, NP, Real, InT, OutT, CART>, a, grid, cb * N, smem(cb), st);
+  }
+  static int occupancy(int cb) {
+    return blocks_per_sm(stage_kernel<DIM, NP, Real, InT, OutT, CART>, cb * N, smem(cb));
+  }
+};
+
+template <typename Real, typename InT, typename OutT, bool CART, bool POST>
+struct CkK {
+  static size_t smem(int cb) { return (size_t)CkSmem<DIM, NP, CART>(cb).end * sizeof(Real); }
+  static cudaError_t launch(const LaunchArgs& a, int grid, cudaStream_t st) {
+    const int cb = a.cells_per_block;
+    return run(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST>, a, grid, cb * N, smem(cb), st);
+  }
+  static int occupancy(int cb) {
+    return blocks_per_sm(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST>, cb * N, smem(cb));
+  }
+};
+
+template <class K>
+void fill(KernelEntry& e) {
+  e.launch = &K::launch;
+  e.occupancy = &K::occupancy;
+  e.smem = &K::smem;
+}
+
+}  // namespace
+
+#define EW_CAT2(a, b, c) a##b##_##c
+#define EW_CAT(a, b, c) EW_CAT2(a, b, c)
+#define EW_TABLE_FN EW_CAT(kernel_table_d, EW_DIM, EW_NP)
+
+void EW_TABLE_FN(KernelTable& t) {
+  t.dim = DIM;
+  t.np = NP;
+  t.points = N;
+  // stage kernels: [variant][cart]
+  fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
+  fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);
+  fill<StageK<float, double, float, false>>(t.stage[STAGE_MIX_IN64][0]);
+  fill<StageK<float, double, float, true>>(t.stage[STAGE_MIX_IN64][1]);
+  fill<StageK<float, float, float, false>>(t.stage[STAGE_MIX_IN32][0]);
+  fill<StageK<float, float, float, true>>(t.stage[STAGE_MIX_IN32][1]);
+  // CK kernels: [precision][cart][post]
+  fill<CkK<double, double, double, false, false>>(t.ck[0][0][0]);
+  fill<CkK<double, double, double, false, true>>(t.ck[0][0][1]);
+  fill<CkK<double, double, double, true, false>>(t.ck[0][1][0]);
+  fill<CkK<double, double, double, true, true>>(t.ck[0][1][1]);
+  fill<CkK<float, double, float, false, false>>(t.ck[1][0][0]);
+  fill<CkK<float, double, float, false, true>>(t.ck[1][0][1]);
+  fill<CkK<float, double, float, true, false>>(t.ck[1][1][0]);
+  fill<CkK<float, double, float, true, true>>(t.ck[1][1][1]);
+}
+
+}  // namespace ew

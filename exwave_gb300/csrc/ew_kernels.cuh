@@ -1,0 +1,701 @@
+// ew_kernels.cuh -- the hot-path kernels, templated on dimension, points
+// per direction (NP = k+1), compute precision and storage types.
+//
+//  stage_kernel : one launch = the whole operator M^{-1} A(X) of a stage
+//                 (cell term, element-centric inner faces, boundary faces,
+//                 inverse mass) fused with the epilogue of the integrator:
+//                 plain result (WaveEquationOperation::apply), the two-register
+//                 LSRK update (RKVectorUpdater) or the ADER update
+//                 (ArbitraryHighOrderDG).
+//  ck_kernel    : the ADER Taylor / Cauchy-Kovalevskaya time integral of
+//                 each cell (WaveEquationOperationADER::integrate_taylor_cauchykovalewski),
+//                 optionally starting from the full DG time derivative
+//                 (use_ader_post), fused with the operator for that case.
+//
+// Thread mapping: one thread per Gauss point, CB cells per CTA, a
+// grid-stride loop over a work list of cell blocks (one solve or many).
+// Each CTA stages its cells' input in shared memory; a face reads the
+// neighbour's values along the lines normal to the face from shared memory
+// when the neighbour is in the same block and from L2 otherwise, so each
+// vector is streamed from HBM about once per stage.
+#pragma once
+
+#include "ew_device.cuh"
+
+namespace ew {
+
+template <int DIM, int NP, bool CART>
+struct Shape {
+  static constexpr int N = ipow_c(NP, DIM);
+  static constexpr int NF = ipow_c(NP, DIM - 1);
+  static constexpr int F = DIM + 1;
+  static constexpr int NV = 1 << DIM;
+  static constexpr int FF = CART ? 2 : DIM + 1;   // flux values kept per face point
+  static constexpr int GEO = CART ? DIM : NV * DIM;
+  static constexpr int BAS = (basis_total(NP) + 3) & ~3;
+};
+
+// Shared-memory layout in units of Real.
+template <int DIM, int NP, bool CART>
+struct OpSmem {
+  using S = Shape<DIM, NP, CART>;
+  int basis, X, G, Fl, geo, mat, end;
+  __host__ __device__ explicit OpSmem(int CB) {
+    basis = 0;
+    X = S::BAS;
+    G = X + CB * S::F * S::N;
+    Fl = G + CB * DIM * S::N;
+    geo = Fl + CB * 2 * DIM * S::FF * S::NF;
+    mat = geo + CB * S::GEO;
+    end = (mat + CB * 2 + 3) & ~3;
+  }
+};
+
+template <int DIM, int NP, bool CART>
+struct CkSmem {
+  using S = Shape<DIM, NP, CART>;
+  OpSmem<DIM, NP, CART> op;
+  int Sv, T1, T2, C[8], end;
+  __host__ __device__ explicit CkSmem(int CB) : op(CB) {
+    Sv = op.end;
+    T1 = Sv + CB * S::F * S::N;
+    T2 = T1 + CB * S::F * S::N;
+    int o = T2 + CB * S::F * S::N;
+    for (int r = 0; r < 8; ++r) C[r] = o;
+    for (int r = 1; r < n_levels(NP); ++r) {
+      C[r] = o;
+      o += CB * S::F * ipow_c(NP - 2 * r, DIM);
+    }
+    end = (o + 3) & ~3;
+  }
+};
+
+template <typename Real, typename T>
+__device__ __forceinline__ Real to_real(T v) {
+  if constexpr (sizeof(Real) == 4 && sizeof(T) == 8) {
+    return f64_to_f32(v);
+  } else {
+    return static_cast<Real>(v);
+  }
+}
+
+__device__ __forceinline__ int dir_stride(int e, int NP) { return e == 0 ? 1 : (e == 1 ? NP : NP * NP); }
+
+// Copy the input of the block's cells, their geometry and materials into
+// shared memory.
+template <int DIM, int NP, typename Real, typename InT, bool CART>
+__device__ __forceinline__ void load_block(const SolveDesc& sd, int cell_begin, int nc, Real* sX,
+                                           Real* sGeo, Real* sMat) {
+  using S = Shape<DIM, NP, CART>;
+  const InT* X = static_cast<const InT*>(sd.X) + (size_t)cell_begin * S::F * S::N;
+  const int total = nc * S::F * S::N;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) sX[i] = to_real<Real>(load_nc(X + i));
+  const Real* G = static_cast<const Real*>(sd.geo) + (size_t)cell_begin * S::GEO;
+  for (int i = threadIdx.x; i < nc * S::GEO; i += blockDim.x) sGeo[i] = load_nc(G + i);
+  const Real* M = static_cast<const Real*>(sd.mat) + (size_t)cell_begin * 2;
+  for (int i = threadIdx.x; i < nc * 2; i += blockDim.x) sMat[i] = load_nc(M + i);
+}
+
+// Cell term at point q of local cell cl: returns the velocity part
+// (already divided by JxW) and 1/JxW; writes the contravariant pressure
+// flux G_e = bf rho c^2 JxW (J^{-T} u)_e to sG.  evaluate_cell,
+// wave_equation_operations.cc:424-456.
+template <int DIM, int NP, typename Real, bool CART>
+__device__ __forceinline__ void op_cell(const Real* sB, const Real* sX, Real* sG, const Real* sGeo,
+                                        const Real* sMat, int cl, int q, Real bf, Real* Ru,
+                                        Real& inv_jxw) {
+  using S = Shape<DIM, NP, CART>;
+  const Level<Real> L = get_level(sB, NP, 0);
+  int i[3] = {0, 0, 0};
+  split_point<DIM, NP>(q, i);
+  const Real* x = sX + cl * S::F * S::N;
+  const Real* p = x + DIM * S::N;
+  Real gxi[DIM];
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) {
+    const int str = ipow_c(NP, e);
+    const Real* row = L.D + i[e] * NP;
+    const Real* line = p + q - i[e] * str;
+    Real s = Real(0);
+#pragma unroll
+    for (int a = 0; a < NP; ++a) s += row[a] * line[a * str];
+    gxi[e] = s;
+  }
+  Real xi[DIM];
+  Real W = Real(1);
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) {
+    xi[e] = L.x[i[e]];
+    W *= L.w[i[e]];
+  }
+  Real JiT[DIM][DIM];
+  const Real det = cell_geom<DIM, Real, CART>(sGeo + cl * S::GEO, xi, JiT);
+  const Real jxw = det * W;
+  inv_jxw = Real(1) / jxw;
+  const Real rho = sMat[2 * cl], c = sMat[2 * cl + 1];
+  const Real fu = -bf / rho;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    Real g = Real(0);
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) g += JiT[d][e] * gxi[e];
+    Ru[d] = fu * g;
+  }
+  const Real fp = bf * rho * c * c * jxw;
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) {
+    Real s = Real(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) s += JiT[d][e] * x[d * S::N + q];
+    sG[cl * DIM * S::N + e * S::N + q] = fp * s;
+  }
+}
+
+// Flux at face point fp of the block (all faces of all cells of the block),
+// times the face JxW, into sFl.  evaluate_inner_face (wave_equation_operations.cc:480-551)
+// seen from this cell's side, and evaluate_boundary_face (569-629).
+template <int DIM, int NP, typename Real, typename InT, bool CART>
+__device__ __forceinline__ void op_face(const Real* sB, const Real* sX, Real* sFl, const Real* sGeo,
+                                        const Real* sMat, const SolveDesc& sd, int cell_begin,
+                                        int nc, int fp, Real bf, int* err) {
+  using S = Shape<DIM, NP, CART>;
+  constexpr int F = S::F, N = S::N, NF = S::NF;
+  const Level<Real> L = get_level(sB, NP, 0);
+  const int cl = fp / (2 * DIM * NF);
+  const int rem = fp - cl * 2 * DIM * NF;
+  const int f = rem / NF;
+  const int t = rem - f * NF;
+  const int e = f >> 1, s = f & 1;
+  int ti[3] = {0, 0, 0};
+  const int q0 = face_base<DIM, NP>(e, t, ti);
+  const int str = dir_stride(e, NP);
+  const Real* Ls = s ? L.L1 : L.L0;
+  const Real* Lm = s ? L.L0 : L.L1;
+  const Real* x = sX + cl * F * N;
+  const Real sgn = s ? Real(1) : Real(-1);
+
+  // own trace
+  Real vp[F];
+#pragma unroll
+  for (int fld = 0; fld < F; ++fld) {
+    vp[fld] = Real(0);
+    if (CART && fld != e && fld != DIM) continue;
+    Real a = Real(0);
+#pragma unroll
+    for (int j = 0; j < NP; ++j) a += Ls[j] * x[fld * N + q0 + j * str];
+    vp[fld] = a;
+  }
+  // normal and face JxW
+  Real nrm[DIM];
+  Real jxw_f;
+  if constexpr (CART) {
+    const Real* h = sGeo + cl * S::GEO;
+    Real area = Real(1);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      nrm[d] = (d == e) ? sgn : Real(0);
+      if (d != e) area *= h[d] * L.w[ti[d]];
+    }
+    jxw_f = area;
+  } else {
+    Real xi[DIM];
+    Real wt = Real(1);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      if (d == e) {
+        xi[d] = s ? Real(1) : Real(0);
+      } else {
+        xi[d] = L.x[ti[d]];
+        wt *= L.w[ti[d]];
+      }
+    }
+    Real JiT[DIM][DIM];
+    const Real det = geom_general<DIM, Real>(sGeo + cl * S::GEO, xi, JiT);
+    Real len2 = Real(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      nrm[d] = sgn * JiT[d][e];
+      len2 += nrm[d] * nrm[d];
+    }
+    const Real len = sqrt(len2);
+    const Real il = Real(1) / len;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) nrm[d] *= il;
+    jxw_f = wt * fabs(det) * len;
+  }
+  const Real rho = sMat[2 * cl], c = sMat[2 * cl + 1];
+  const Real rho_inv = Real(1) / rho, c_sq = c * c;
+  const Real tau_p = Real(1) / (c * rho);
+  Real un_p = Real(0);
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) un_p += vp[d] * nrm[d];
+
+  const int cell = cell_begin + cl;
+  int nb = sd.nbr[(size_t)cell * 2 * DIM + f];
+  Real lambda;
+  Real tau_here = tau_p;
+  if (nb >= 0) {
+    if (nb >= sd.n_cells) {
+      atomicOr(err, ERR_BAD_NEIGHBOR);
+      nb = cell;
+    }
+    Real vm[F];
+    Real rho_m, c_m;
+    const int nl = nb - cell_begin;
+    if (nl >= 0 && nl < nc) {
+      const Real* xm = sX + nl * F * N;
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        vm[fld] = Real(0);
+        if (CART && fld != e && fld != DIM) continue;
+        Real a = Real(0);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) a += Lm[j] * xm[fld * N + q0 + j * str];
+        vm[fld] = a;
+      }
+      rho_m = sMat[2 * nl];
+      c_m = sMat[2 * nl + 1];
+    } else {
+      const InT* xm = static_cast<const InT*>(sd.X) + (size_t)nb * F * N;
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        vm[fld] = Real(0);
+        if (CART && fld != e && fld != DIM) continue;
+        Real a = Real(0);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) a += Lm[j] * to_real<Real>(load_nc(xm + fld * N + q0 + j * str));
+        vm[fld] = a;
+      }
+      const Real* M = static_cast<const Real*>(sd.mat);
+      rho_m = load_nc(M + 2 * (size_t)nb);
+      c_m = load_nc(M + 2 * (size_t)nb + 1);
+    }
+    Real un_m = Real(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) un_m -= vm[d] * nrm[d];
+    const Real tau_m = Real(1) / (c_m * rho_m);
+    const Real tau_inv = Real(1) / (tau_p + tau_m);
+    lambda = tau_inv * (un_p + un_m + tau_p * vp[DIM] + tau_m * vm[DIM]);
+  } else {
+    const int id = -nb;
+    if (id == EW_BC_SOFT_WALL_ID) {
+      lambda = un_p / tau_p + vp[DIM];
+    } else if (id == EW_BC_ABSORBING_ID) {
+      const Real tsum = tau_p + Real(1) / (c * rho);
+      lambda = tau_p / tsum * vp[DIM] + Real(1) / tsum * un_p;
+    } else {
+      if (id != EW_BC_HARD_WALL_ID) atomicOr(err, ERR_BAD_BOUNDARY_ID);
+      lambda = Real(0);
+    }
+  }
+  const Real scale = bf * jxw_f;
+  const Real pd = (vp[DIM] - lambda) * rho_inv * scale;
+  const Real fpres = c_sq * rho * (-un_p + tau_here * (lambda - vp[DIM])) * scale;
+  Real* out = sFl + (cl * 2 * DIM + f) * S::FF * NF + t;
+  if constexpr (CART) {
+    out[0] = pd * nrm[e];
+    out[NF] = fpres;
+  } else {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) out[d * NF] = pd * nrm[d];
+    out[DIM * NF] = fpres;
+  }
+}
+
+// Gather of the cell term's pressure part, the face lifts and the inverse
+// mass at point q: k = M^{-1} A(X) at that point (inverse mass:
+// local_apply_mass_matrix, wave_equation_operations.cc:633-661).
+template <int DIM, int NP, typename Real, bool CART>
+__device__ __forceinline__ void op_collect(const Real* sB, const Real* sG, const Real* sFl, int cl,
+                                           int q, const Real* Ru, Real inv_jxw, Real* k) {
+  using S = Shape<DIM, NP, CART>;
+  constexpr int N = S::N, NF = S::NF;
+  const Level<Real> L = get_level(sB, NP, 0);
+  int i[3] = {0, 0, 0};
+  split_point<DIM, NP>(q, i);
+  Real rp = Real(0);
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) {
+    const int str = ipow_c(NP, e);
+    const Real* g = sG + cl * DIM * N + e * N + q - i[e] * str;
+#pragma unroll
+    for (int a = 0; a < NP; ++a) rp += L.D[a * NP + i[e]] * g[a * str];
+  }
+  Real lift[DIM + 1];
+#pragma unroll
+  for (int fld = 0; fld <= DIM; ++fld) lift[fld] = Real(0);
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) {
+    const int t = face_index<DIM, NP>(i, e);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const Real l = s ? L.L1[i[e]] : L.L0[i[e]];
+      const Real* fl = sFl + (cl * 2 * DIM + 2 * e + s) * S::FF * NF + t;
+      if constexpr (CART) {
+        lift[e] += l * fl[0];
+        lift[DIM] += l * fl[NF];
+      } else {
+#pragma unroll
+        for (int fld = 0; fld <= DIM; ++fld) lift[fld] += l * fl[fld * NF];
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) k[d] = Ru[d] + lift[d] * inv_jxw;
+  k[DIM] = (rp + lift[DIM]) * inv_jxw;
+}
+
+template <typename Real>
+__device__ __forceinline__ void load_basis(const void* basis, Real* sB, int n) {
+  const Real* b = static_cast<const Real*>(basis);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sB[i] = b[i];
+}
+
+__device__ __forceinline__ const SolveDesc& pick(const LaunchArgs& La, int solve) {
+  return La.solves ? La.solves[solve] : La.single;
+}
+
+// ============================================================ stage kernel
+template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART>
+__global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
+  using S = Shape<DIM, NP, CART>;
+  constexpr int F = S::F, N = S::N;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* sm = reinterpret_cast<Real*>(smem_raw);
+  const int CB = La.cells_per_block;
+  const OpSmem<DIM, NP, CART> lay(CB);
+  Real* sB = sm + lay.basis;
+  Real* sX = sm + lay.X;
+  Real* sG = sm + lay.G;
+  Real* sFl = sm + lay.Fl;
+  Real* sGeo = sm + lay.geo;
+  Real* sMat = sm + lay.mat;
+  if ((int)blockDim.x != CB * N) {
+    if (threadIdx.x == 0) atomicOr(La.err, ERR_BAD_LAUNCH);
+    return;
+  }
+  load_basis<Real>(La.basis, sB, basis_total(NP));
+
+  for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
+    const WorkItem wi = La.work[w];
+    const SolveDesc& sd = pick(La, wi.solve);
+    const int nc = wi.n_cells;
+    __syncthreads();  // previous item done with shared memory; basis loaded
+    load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
+    __syncthreads();
+    const Real bf = static_cast<Real>(sd.bf);
+    const int cl = threadIdx.x / N;
+    const int q = threadIdx.x - cl * N;
+    const bool active = cl < nc;
+    Real Ru[DIM];
+    Real inv_jxw = Real(1);
+    if (active) op_cell<DIM, NP, Real, CART>(sB, sX, sG, sGeo, sMat, cl, q, bf, Ru, inv_jxw);
+    for (int fp = threadIdx.x; fp < nc * 2 * DIM * S::NF; fp += blockDim.x)
+      op_face<DIM, NP, Real, InT, CART>(sB, sX, sFl, sGeo, sMat, sd, wi.cell_begin, nc, fp, bf,
+                                        La.err);
+    __syncthreads();
+    if (!active) continue;
+    Real k[F];
+    op_collect<DIM, NP, Real, CART>(sB, sG, sFl, cl, q, Ru, inv_jxw, k);
+
+    const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + q;
+    const int mode = sd.mode;
+    if (mode == MODE_APPLY) {
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) sd.Aout[g0 + fld * N] = static_cast<double>(k[fld]);
+    } else if (mode == MODE_RK_MID) {
+      OutT* Xo = static_cast<OutT*>(sd.Xout);
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        const size_t g = g0 + fld * N;
+        const double a = sd.A[g];
+        if constexpr (sizeof(Real) == 8) {
+          const double xn = a + sd.f1 * k[fld];
+          Xo[g] = static_cast<OutT>(xn);
+          sd.Aout[g] = xn + sd.f2 * k[fld];
+        } else {
+          const float kf = k[fld];
+          Xo[g] = static_cast<OutT>(fmaf(sd.f1f, kf, f64_to_f32(a)));
+          sd.Aout[g] = a + f32_to_f64(fmaf(sd.fb_hi, kf, sd.fb_lo * kf));
+        }
+      }
+    } else {  // MODE_RK_LAST
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        const size_t g = g0 + fld * N;
+        const double a = sd.A[g];
+        if constexpr (sizeof(Real) == 8) {
+          sd.Aout[g] = a + sd.f1 * k[fld];
+        } else {
+          const float kf = k[fld];
+          sd.Aout[g] = a + f32_to_f64(fmaf(sd.f1_hi, kf, sd.f1_lo * kf));
+        }
+      }
+    }
+  }
+}
+
+// ============================================================ CK kernel
+// One sweep of a 1D matrix M (rows x cols) along direction e over the
+// tensors of nc cells x F fields.  in/out: [cell][field][points] with
+// per-cell stride cs and per-field stride equal to the tensor size.
+template <int DIM, typename Real>
+__device__ __forceinline__ void sweep(const Real* M, int rows, int cols, int e, const int* ext_in,
+                                      const Real* in, int cs_in, Real* out, int cs_out, int nc,
+                                      int nfields) {
+  int ext_out[3] = {ext_in[0], ext_in[1], ext_in[2]};
+  ext_out[e] = rows;
+  int tin = 1, tout = 1;
+  for (int d = 0; d < DIM; ++d) {
+    tin *= ext_in[d];
+    tout *= ext_out[d];
+  }
+  const int total = nc * nfields * tout;
+  const int str_in = (e == 0) ? 1 : (e == 1 ? ext_in[0] : ext_in[0] * ext_in[1]);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int cl = idx / (nfields * tout);
+    const int r = idx - cl * nfields * tout;
+    const int fld = r / tout;
+    const int p = r - fld * tout;
+    int o[3] = {0, 0, 0};
+    {
+      int tt = p;
+      for (int d = 0; d < DIM; ++d) {
+        o[d] = tt % ext_out[d];
+        tt /= ext_out[d];
+      }
+    }
+    int base = 0, str = 1;
+    for (int d = 0; d < DIM; ++d) {
+      if (d != e) base += o[d] * str;
+      str *= ext_in[d];
+    }
+    const Real* src = in + cl * cs_in + fld * tin + base;
+    const Real* mrow = M + o[e] * cols;
+    Real s = Real(0);
+    for (int j = 0; j < cols; ++j) s += mrow[j] * src[j * str_in];
+    out[cl * cs_out + fld * tout + p] = s;
+  }
+}
+
+// Apply a 1D matrix in all DIM directions (rows x cols per direction).
+// Result lands in `dst` (which may alias `src` only when DIM sweeps end
+// there); t1, t2 are scratch.  Contains __syncthreads.
+template <int DIM, typename Real>
+__device__ __forceinline__ void tensor_all(const Real* M, int rows, int cols, const Real* src,
+                                           int cs_src, Real* dst, int cs_dst, Real* t1, Real* t2,
+                                           int cs_t, int nc, int nfields) {
+  int ext[3] = {cols, cols, cols};
+  if constexpr (DIM == 2) {
+    sweep<DIM, Real>(M, rows, cols, 0, ext, src, cs_src, t1, cs_t, nc, nfields);
+    __syncthreads();
+    ext[0] = rows;
+    sweep<DIM, Real>(M, rows, cols, 1, ext, t1, cs_t, dst, cs_dst, nc, nfields);
+    __syncthreads();
+  } else {
+    sweep<DIM, Real>(M, rows, cols, 0, ext, src, cs_src, t1, cs_t, nc, nfields);
+    __syncthreads();
+    ext[0] = rows;
+    sweep<DIM, Real>(M, rows, cols, 1, ext, t1, cs_t, t2, cs_t, nc, nfields);
+    __syncthreads();
+    ext[1] = rows;
+    sweep<DIM, Real>(M, rows, cols, 2, ext, t2, cs_t, dst, cs_dst, nc, nfields);
+    __syncthreads();
+  }
+}
+
+// Derivative of the field set S (level r, m points per direction) at point
+// qq of cell cl: out_u_d = rho^{-1} d_d S_p, out_p = rho c^2 div S_u
+// (integrate_taylor_cauchykovalewski_step, wave_equation_operations.cc:1096-1197).
+template <int DIM, int NP, typename Real, bool CART>
+__device__ __forceinline__ void ck_derivative(const Level<Real>& L, const Real* Sv, const Real* sGeo,
+                                              Real rho, Real c_sq, int qq, Real* out) {
+  using Sh = Shape<DIM, NP, CART>;
+  const int m = L.m;
+  int Nm = m;
+  for (int d = 1; d < DIM; ++d) Nm *= m;
+  int i[3] = {0, 0, 0};
+  {
+    int t = qq;
+    for (int d = 0; d < DIM; ++d) {
+      i[d] = t % m;
+      t /= m;
+    }
+  }
+  Real g[DIM + 1][DIM];
+#pragma unroll
+  for (int fld = 0; fld <= DIM; ++fld) {
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) {
+      const int str = (e == 0) ? 1 : (e == 1 ? m : m * m);
+      const Real* row = L.D + i[e] * m;
+      const Real* line = Sv + fld * Nm + qq - i[e] * str;
+      Real s = Real(0);
+      for (int a = 0; a < m; ++a) s += row[a] * line[a * str];
+      g[fld][e] = s;
+    }
+  }
+  Real xi[DIM];
+#pragma unroll
+  for (int e = 0; e < DIM; ++e) xi[e] = L.x[i[e]];
+  Real JiT[DIM][DIM];
+  cell_geom<DIM, Real, CART>(sGeo, xi, JiT);
+  Real div = Real(0);
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) div += g[d][e] * JiT[d][e];
+  const Real rho_inv = Real(1) / rho;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    Real pg = Real(0);
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) pg += g[DIM][e] * JiT[d][e];
+    out[d] = rho_inv * pg;
+  }
+  out[DIM] = c_sq * rho * div;
+  (void)sizeof(Sh);
+}
+
+template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST>
+__global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
+  using S = Shape<DIM, NP, CART>;
+  constexpr int F = S::F, N = S::N;
+  constexpr int NL = n_levels(NP);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* sm = reinterpret_cast<Real*>(smem_raw);
+  const int CB = La.cells_per_block;
+  const CkSmem<DIM, NP, CART> lay(CB);
+  Real* sB = sm + lay.op.basis;
+  Real* sX = sm + lay.op.X;
+  Real* sG = sm + lay.op.G;
+  Real* sFl = sm + lay.op.Fl;
+  Real* sGeo = sm + lay.op.geo;
+  Real* sMat = sm + lay.op.mat;
+  Real* sS = sm + lay.Sv;
+  Real* sT1 = sm + lay.T1;
+  Real* sT2 = sm + lay.T2;
+  if ((int)blockDim.x != CB * N) {
+    if (threadIdx.x == 0) atomicOr(La.err, ERR_BAD_LAUNCH);
+    return;
+  }
+  load_basis<Real>(La.basis, sB, basis_total(NP));
+  const double dt = La.dt;
+  // Taylor terms j = 0..max(k,2); derivatives j >= 2 come from the
+  // recursive steps s = 0..n_steps-1.
+  const int n_steps = (NP - 2 > 1) ? NP - 2 : 1;
+
+  for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
+    const WorkItem wi = La.work[w];
+    const SolveDesc& sd = pick(La, wi.solve);
+    const int nc = wi.n_cells;
+    __syncthreads();
+    load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
+    for (int r = 1; r < NL; ++r) {
+      const int sz = nc * F * ipow_c(NP - 2 * r, DIM);
+      for (int i = threadIdx.x; i < sz; i += blockDim.x) sm[lay.C[r] + i] = Real(0);
+    }
+    __syncthreads();
+    const int cl = threadIdx.x / N;
+    const int q = threadIdx.x - cl * N;
+    const bool active = cl < nc;
+    const Real rho = active ? sMat[2 * cl] : Real(1);
+    const Real cc = active ? sMat[2 * cl + 1] : Real(1);
+    const Real c_sq = cc * cc;
+    Real d1[F];
+    if constexpr (POST) {
+      // first time derivative = full DG operator (recongraddiv = apply(src))
+      Real Ru[DIM];
+      Real inv_jxw = Real(1);
+      if (active) op_cell<DIM, NP, Real, CART>(sB, sX, sG, sGeo, sMat, cl, q, Real(1), Ru, inv_jxw);
+      for (int fp = threadIdx.x; fp < nc * 2 * DIM * S::NF; fp += blockDim.x)
+        op_face<DIM, NP, Real, InT, CART>(sB, sX, sFl, sGeo, sMat, sd, wi.cell_begin, nc, fp,
+                                          Real(1), La.err);
+      __syncthreads();
+      if (active) op_collect<DIM, NP, Real, CART>(sB, sG, sFl, cl, q, Ru, inv_jxw, d1);
+    } else {
+      if (active) {
+        Real o[F];
+        ck_derivative<DIM, NP, Real, CART>(get_level(sB, NP, 0), sX + cl * F * N,
+                                           sGeo + cl * S::GEO, rho, c_sq, q, o);
+#pragma unroll
+        for (int fld = 0; fld < F; ++fld) d1[fld] = -o[fld];
+      }
+    }
+    // Taylor terms 0 and 1; the recursion starts from S = -du/dt
+    Real c0[F];
+    const Real dtr = static_cast<Real>(dt);
+    const Real half_dt2 = static_cast<Real>(0.5 * dt * dt);
+    if (active) {
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        c0[fld] = dtr * sX[cl * F * N + fld * N + q] + half_dt2 * d1[fld];
+        sS[cl * F * N + fld * N + q] = -d1[fld];
+      }
+    }
+    __syncthreads();
+    double fac = -0.5;
+    double dtp = dt * dt * dt;
+    for (int s = 0; s < n_steps; ++s) {
+      const int r = s / 2;
+      const Level<Real> L = get_level(sB, NP, r);
+      const int m = L.m;
+      const int Nm = ipow_rt(m, DIM);
+      fac /= -(s + 3.0);  // fac = -1/2 prod_{j=2}^{s+2} (-1/(j+1))
+      if (s > 0) dtp *= dt;  // dt^(s+3)
+      const Real fac_t = static_cast<Real>(fac * dtp);
+      Real sn[F];
+      const bool act_l = active && q < Nm;
+      if (act_l)
+        ck_derivative<DIM, NP, Real, CART>(L, sS + cl * F * N, sGeo + cl * S::GEO, rho, c_sq, q, sn);
+      __syncthreads();
+      if (act_l) {
+#pragma unroll
+        for (int fld = 0; fld < F; ++fld) {
+          sS[cl * F * N + fld * Nm + q] = sn[fld];
+          if (r == 0)
+            c0[fld] += fac_t * sn[fld];
+          else
+            sm[lay.C[r] + cl * F * Nm + fld * Nm + q] += fac_t * sn[fld];
+        }
+      }
+      __syncthreads();
+      if (s + 1 < n_steps && (s & 1)) {
+        // L2 projection of S onto the next lower level (degree - 2)
+        const Level<Real> Ln = get_level(sB, NP, r + 1);
+        tensor_all<DIM, Real>(Ln.P, Ln.m, m, sS, F * N, sS, F * N, sT1, sT2, F * N, nc, F);
+      }
+    }
+    // interpolate the lower-level contributions back up and sum
+    const int r_last = (n_steps - 1) / 2;
+    for (int r = r_last; r >= 1; --r) {
+      const Level<Real> Lr = get_level(sB, NP, r);
+      const int m = Lr.m, mp = m + 2;
+      const int Nmp = ipow_rt(mp, DIM);
+      Real* up = (DIM == 2) ? sT2 : sT1;
+      tensor_all<DIM, Real>(Lr.E, mp, m, sm + lay.C[r], F * ipow_rt(m, DIM), up, F * N, sT1, sT2,
+                            F * N, nc, F);
+      if (r - 1 == 0) {
+        if (active) {
+#pragma unroll
+          for (int fld = 0; fld < F; ++fld) c0[fld] += up[cl * F * N + fld * Nmp + q];
+        }
+      } else {
+        for (int idx = threadIdx.x; idx < nc * F * Nmp; idx += blockDim.x) {
+          const int c2 = idx / (F * Nmp);
+          const int rr = idx - c2 * F * Nmp;
+          sm[lay.C[r - 1] + c2 * F * Nmp + rr] += up[c2 * F * N + rr];
+        }
+      }
+      __syncthreads();
+    }
+    if (active) {
+      OutT* T = static_cast<OutT*>(sd.Xout);
+      const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + q;
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) T[g0 + fld * N] = static_cast<OutT>(c0[fld]);
+    }
+  }
+}
+
+}  // namespace ew

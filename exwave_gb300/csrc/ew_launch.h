@@ -1,0 +1,36 @@
+// ew_launch.h -- table of kernel launchers per (dimension, degree), filled
+// by the instantiation units (ew_inst.cu compiled once per pair).
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "ew_device.cuh"
+
+namespace ew {
+
+enum StageVariant : int {
+  STAGE_F64 = 0,       // FP64 operator, FP64 input and output
+  STAGE_MIX_IN64 = 1,  // FP32 operator reading an FP64 input (first stage, apply)
+  STAGE_MIX_IN32 = 2,  // FP32 operator reading an FP32 stage input
+  N_STAGE_VARIANTS = 3
+};
+
+struct KernelEntry {
+  cudaError_t (*launch)(const LaunchArgs&, int grid, cudaStream_t) = nullptr;
+  int (*occupancy)(int cells_per_block) = nullptr;
+  size_t (*smem)(int cells_per_block) = nullptr;
+};
+
+struct KernelTable {
+  int dim = 0, np = 0, points = 0;
+  KernelEntry stage[N_STAGE_VARIANTS][2];  // [variant][cartesian]
+  KernelEntry ck[2][2][2];                 // [mixed][cartesian][post]
+};
+
+#define EW_DECL(d, n) void kernel_table_d##d##_##n(KernelTable&);
+EW_DECL(2, 2) EW_DECL(2, 3) EW_DECL(2, 4) EW_DECL(2, 5) EW_DECL(2, 6) EW_DECL(2, 7) EW_DECL(2, 8)
+EW_DECL(3, 2) EW_DECL(3, 3) EW_DECL(3, 4) EW_DECL(3, 5) EW_DECL(3, 6) EW_DECL(3, 7) EW_DECL(3, 8)
+#undef EW_DECL
+
+}  // namespace ew

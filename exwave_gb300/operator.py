@@ -1,0 +1,152 @@
+"""WaveEquationOperation on the GPU: the host-side mirror of the reference's
+``WaveEquationOperationBase<dim>`` (wave_equation_operations.h:56-98) over
+the C ABI.  Vectors are FP64 CUDA tensors in the canonical layout
+[cell][field][Gauss point] (fields u_0..u_{d-1}, p).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+PRECISIONS = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED}
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not (t.is_cuda and t.is_contiguous()):
+        raise ValueError("expected a contiguous CUDA tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _modes(amps, kvecs):
+    amps = np.ascontiguousarray(amps, dtype=np.float64)
+    kv = np.zeros((len(amps), 3), dtype=np.int32)
+    kv[:, :len(kvecs[0])] = np.asarray(kvecs, dtype=np.int32)
+    return amps, kv
+
+
+class WaveEquationOperation:
+    """Operator of one solve: ``apply`` (RK), ``apply_ader`` (ADER), the
+    fused integrator steps, initial fields and L2 errors."""
+
+    def __init__(self, mesh, degree, precision="fp64", use_ader_post=False, cells_per_block=0,
+                 device=0):
+        import torch
+        self.torch = torch
+        self.L = _lib.load()
+        self.mesh = mesh
+        self.dim = mesh.dim
+        self.degree = degree
+        self.precision = precision
+        self.use_ader_post = bool(use_ader_post)
+        self.device = device
+        self._keep = [np.ascontiguousarray(mesh.vertices, np.float64),
+                      np.ascontiguousarray(mesh.neighbors, np.int32),
+                      np.ascontiguousarray(mesh.speed, np.float64),
+                      np.ascontiguousarray(mesh.density, np.float64)]
+        md = _lib.MeshDesc()
+        md.dim = mesh.dim
+        md.degree = degree
+        md.n_cells = mesh.n_cells
+        md.vertices = self._keep[0].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        md.neighbors = self._keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        md.speed = self._keep[2].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        md.density = self._keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        op = _lib.Options()
+        op.precision = PRECISIONS[precision]
+        op.use_ader_post = int(self.use_ader_post)
+        op.spectral_evaluation = 1
+        op.cells_per_block = cells_per_block
+        op.device = device
+        h = ctypes.c_void_p()
+        _lib.check(self.L.ew_create(ctypes.byref(md), ctypes.byref(op), ctypes.byref(h)))
+        self.ctx = h
+        self.n_dofs = self.L.ew_n_dofs(h)
+        self.n_cells = mesh.n_cells
+        self.points = (degree + 1) ** mesh.dim
+
+    def Name(self):
+        return "ADER" if self.use_ader_post else "Runge-Kutta"
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.ew_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        _lib.check(rc, self.ctx)
+
+    def set_stream(self, stream):
+        self._chk(self.L.ew_set_stream(self.ctx, ctypes.c_void_p(stream.cuda_stream)))
+
+    def new_vector(self):
+        return self.torch.zeros(self.n_dofs, dtype=self.torch.float64,
+                                device="cuda:%d" % self.device)
+
+    # -- reference interface -------------------------------------------
+    def apply(self, src, dst):
+        self._chk(self.L.ew_apply(self.ctx, _ptr(src), _ptr(dst)))
+
+    def apply_ader(self, src, dst, dt):
+        self._chk(self.L.ew_apply_ader(self.ctx, dt, _ptr(src), _ptr(dst)))
+
+    def rk_update(self, f1, f2, is_last, v1, v2, v3):
+        self._chk(self.L.ew_rk_update(self.ctx, f1, f2, int(is_last), _ptr(v1), _ptr(v2), _ptr(v3)))
+
+    def lsrk45_step(self, dt, vec_n, vec_np):
+        self._chk(self.L.ew_lsrk45_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
+
+    def ader_step(self, dt, vec_n, vec_np):
+        self._chk(self.L.ew_ader_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
+
+    def quadrature_points(self):
+        out = self.torch.zeros(self.n_cells * self.points * self.dim, dtype=self.torch.float64,
+                               device="cuda:%d" % self.device)
+        self._chk(self.L.ew_quadrature_points(self.ctx, _ptr(out)))
+        return out.view(self.n_cells, self.points, self.dim)
+
+    def project_membrane(self, amps, kvecs, t=0.0, out=None):
+        a, kv = _modes(amps, kvecs)
+        out = self.new_vector() if out is None else out
+        self._chk(self.L.ew_project_membrane(self.ctx, len(a), a.ctypes.data, kv.ctypes.data, t,
+                                             _ptr(out)))
+        return out
+
+    def project_gaussian(self, x0, width, amp=1.0, out=None):
+        c = np.zeros(3)
+        c[:len(x0)] = x0
+        out = self.new_vector() if out is None else out
+        self._chk(self.L.ew_project_gaussian(self.ctx, c.ctypes.data, width, amp, _ptr(out)))
+        return out
+
+    def l2_errors(self, u, amps, kvecs, t):
+        a, kv = _modes(amps, kvecs)
+        out = np.zeros(3)
+        self._chk(self.L.ew_l2_errors_membrane(self.ctx, _ptr(u), len(a), a.ctypes.data,
+                                               kv.ctypes.data, t, out.ctypes.data))
+        return out
+
+    def l2_difference(self, a, b):
+        out = np.zeros(2)
+        self._chk(self.L.ew_l2_difference(self.ctx, _ptr(a), _ptr(b), out.ctypes.data))
+        return out
+
+    def synchronize(self):
+        self._chk(self.L.ew_synchronize(self.ctx))
+
+    def kernel_launches(self):
+        return self.L.ew_kernel_launches(self.ctx)
+
+
+def reference_mode(dim, m):
+    """The reference's single membrane mode (input_parameters.h:95-128): wave
+    number m in every direction, unit amplitude."""
+    return [1.0], [[m] * dim]

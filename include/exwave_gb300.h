@@ -1,0 +1,185 @@
+/* exwave_gb300.h -- C ABI of the GB300-native ExWave DG operator hot path.
+ *
+ * The library re-implements, as CUDA kernels for sm_103a, the explicit
+ * upwind DG operator of ExWave (kronbichler/exwave) for the first-order
+ * acoustic system (pressure p, velocity u) on FE_DGQ(k) quads and hexes,
+ * the low-storage Runge-Kutta stage update around it and the ADER
+ * Taylor / Cauchy-Kovalevskaya time-integral sweep.  Every entry point below
+ * names the reference interface it replaces.
+ *
+ * Conventions shared by all calls
+ *  - State vectors are FP64 device pointers in the canonical layout
+ *    [cell][field][point]: fields u_0..u_{d-1}, p; points are the (k+1)^d
+ *    Gauss points of the cell in lexicographic order (x fastest).  The DG
+ *    solution is stored by its values at the Gauss points (collocation basis
+ *    of QGauss(k+1)), so n_dofs = n_cells * (d+1) * (k+1)^d, as in the
+ *    reference's FE_DGQ(k) system.
+ *  - Every call returns EW_OK (0) or a negative ew_status; no exception
+ *    crosses the ABI.  ew_last_error() gives a message.  Kernels run on the
+ *    context's stream and return asynchronously; ew_synchronize() waits and
+ *    reports device-side errors (bad neighbour index, wait time-out).
+ *  - One context is used by one host thread at a time (the reference's
+ *    operator mutates scratch in const methods as well).
+ */
+#ifndef EXWAVE_GB300_H
+#define EXWAVE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EW_MAX_DEGREE 7 /* k = 1..7 (the reference instantiates 1..12) */
+
+typedef enum ew_status {
+  EW_OK = 0,
+  EW_ERR_INVALID = -1,     /* bad argument or inconsistent mesh */
+  EW_ERR_UNSUPPORTED = -2, /* valid in the reference, not built here */
+  EW_ERR_CUDA = -3,        /* CUDA runtime error */
+  EW_ERR_OOM = -4,         /* device allocation failed */
+  EW_ERR_DEVICE = -5,      /* a kernel raised the device error flag */
+  EW_ERR_TOO_LARGE = -6    /* size above a fixed limit */
+} ew_status;
+
+typedef enum ew_precision {
+  EW_PREC_FP64 = 0, /* operator, geometry and state in FP64 */
+  EW_PREC_MIXED = 1 /* operator and geometry in FP32, state/accumulation FP64 */
+} ew_precision;
+
+typedef enum ew_boundary {
+  EW_BC_SOFT_WALL = 1, /* u.n = 0 */
+  EW_BC_HARD_WALL = 2, /* p = 0 */
+  EW_BC_ABSORBING = 3  /* first-order absorbing condition */
+} ew_boundary;
+
+/* Mesh of one solve, the flattened equivalent of the reference's
+ * MatrixFree setup (WaveEquationOperation::setup / reset_data_vectors,
+ * wave_equation_operations.cc:200-250, 383-400).  Host pointers; copied to the
+ * device by ew_create.
+ *  vertices : [n_cells][2^dim][dim] cell vertices, deal.II lexicographic
+ *             vertex order; cells are multilinear (MappingQGeneric on a flat
+ *             manifold interpolates exactly this map).
+ *  neighbors: [n_cells][2*dim] for face f = 2*direction + side: the index of
+ *             the cell across the face, which must see it as its face f^1
+ *             with the same tangential orientation; or -id for a boundary
+ *             face with boundary id 1, 2 or 3.
+ *  speed, density: [n_cells] material per cell (c, rho). */
+typedef struct ew_mesh_desc {
+  int32_t dim;
+  int32_t degree;
+  int64_t n_cells;
+  const double* vertices;
+  const int32_t* neighbors;
+  const double* speed;
+  const double* density;
+} ew_mesh_desc;
+
+typedef struct ew_options {
+  int32_t precision;           /* ew_precision */
+  int32_t use_ader_post;       /* reference parameter ADER/use_ader_post */
+  int32_t spectral_evaluation; /* reference ADER/spectral_evaluation; only 1 */
+  int32_t cells_per_block;     /* 0: tuned default */
+  int32_t device;              /* CUDA device ordinal */
+} ew_options;
+
+typedef struct ew_ctx ew_ctx;
+
+/* Replaces WaveEquationOperation<dim,k>::setup (wave_equation_operations.cc:200-250)
+ * and the ADER setup (276-315): validates the mesh, flattens geometry and
+ * materials to the device and allocates the operator's scratch. */
+int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** ctx);
+void ew_destroy(ew_ctx* ctx);
+
+/* Message of the last failure on ctx, or of the calling thread's last failed
+ * ew_create when ctx is NULL. */
+const char* ew_last_error(const ew_ctx* ctx);
+
+/* Stream for all later work of ctx (a cudaStream_t; NULL = legacy stream). */
+int ew_set_stream(ew_ctx* ctx, void* stream);
+int64_t ew_n_dofs(const ew_ctx* ctx);
+int64_t ew_n_cells(const ew_ctx* ctx);
+
+/* Replaces WaveEquationOperation::apply (wave_equation_operations.cc:665-685):
+ * dst = M^{-1} A(src), the cell, inner-face and boundary-face terms followed
+ * by the inverse mass matrix, in one kernel. */
+int ew_apply(ew_ctx* ctx, const double* src, double* dst);
+
+/* Replaces RKVectorUpdater::apply_to_subrange (time_integrators.cc:129-155):
+ * not last: v2 += f1*v1; v3 = v2 + f2*v1.  last: v2 = v3 + f1*v1. */
+int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const double* v1,
+                 double* v2, double* v3);
+
+/* Replaces LowStorageRK45Reg2::perform_time_step (time_integrators.cc:235-283):
+ * five fused operator+update stages; on return vec_np holds the new state
+ * and vec_n has been used as a register (its content is undefined), as in
+ * the reference. */
+int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
+
+/* Replaces WaveEquationOperationADER::apply_ader (wave_equation_operations.cc:1346-1381):
+ * T = Taylor time integral of src over [0,dt]; dst = -M^{-1} A(T). */
+int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst);
+
+/* Replaces ArbitraryHighOrderDG::perform_time_step (time_integrators.cc:37-50):
+ * vec_np = vec_n - apply_ader(vec_n), fused into the second ADER kernel. */
+int ew_ader_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np);
+
+/* Physical coordinates of all Gauss points, device pointer [cell][point][dim]
+ * (what FEEvaluation::quadrature_point gives the reference's
+ * project_initial_field, wave_equation_operations.cc:902-935). */
+int ew_quadrature_points(ew_ctx* ctx, double* xyz);
+
+/* Replaces project_initial_field for the vibrating-membrane field: a sum of
+ * modes p = sum A_m cos(w_m t) prod_d sin(k_md pi x_d) with the matching
+ * velocity (c = rho = 1; input_parameters.h:95-128 is the one-mode case).
+ * amp[n_modes], kvec[n_modes][3] are host arrays; u is a device vector. */
+int ew_project_membrane(ew_ctx* ctx, int32_t n_modes, const double* amp, const int32_t* kvec,
+                        double t, double* u);
+
+/* Gaussian pressure pulse p = amp*exp(-|x-x0|^2/(2 width^2)), u = 0. */
+int ew_project_gaussian(ew_ctx* ctx, const double* x0, double width, double amp, double* u);
+
+/* L2 errors against the membrane solution with QGauss(k+2) on the mapped
+ * cells (explicit_wave.cc:439-496): out[0] = |p_h - p|, out[1] = |u_h - u|,
+ * out[2] = |p|.  Synchronises. */
+int ew_l2_errors_membrane(ew_ctx* ctx, const double* u, int32_t n_modes, const double* amp,
+                          const int32_t* kvec, double t, double out[3]);
+
+/* L2 norm of the difference of two states with QGauss(k+2) (pressure,
+ * velocity); used for FP64-vs-mixed comparisons.  Synchronises. */
+int ew_l2_difference(ew_ctx* ctx, const double* a, const double* b, double out[2]);
+
+/* Structured mesh generator: the reference's input_geometry_description
+ * (input_parameters.h:60-88): subdivided_hyper_cube(n_intervals) of [0,1]^dim,
+ * a vertex transform, then n_refinements global refinements with a flat
+ * manifold (new vertices on the multilinear map of each coarse cell).
+ * Cells are numbered lexicographically on the fine grid, x fastest.
+ *  transform 0: the reference's x_0 += f prod_d sin(pi x_d) (input_parameters.h:42-50)
+ *  transform 1: every coordinate x_i += f prod_d sin(2 pi x_d)
+ *  boundary_ids[2*d + s]: id of the domain face x_d = s (s = 0, 1). */
+typedef struct ew_hypercube_desc {
+  int32_t dim;
+  int32_t n_intervals;
+  int32_t n_refinements;
+  int32_t transform;
+  double transform_factor;
+  int32_t boundary_ids[6];
+} ew_hypercube_desc;
+
+int64_t ew_hypercube_n_cells(const ew_hypercube_desc* desc);
+
+/* Fills host arrays vertices[n_cells][2^dim][dim] and
+ * neighbors[n_cells][2*dim] in the ew_mesh_desc conventions. */
+int ew_hypercube_mesh(const ew_hypercube_desc* desc, double* vertices, int32_t* neighbors);
+
+/* Waits for the context's stream and reports a raised device error flag. */
+int ew_synchronize(ew_ctx* ctx);
+
+/* Number of kernels this library has launched on ctx so far. */
+int64_t ew_kernel_launches(const ew_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXWAVE_GB300_H */

@@ -1,0 +1,173 @@
+"""GPU parity: the CUDA kernels, called through the C ABI, against the CPU
+oracle on the same meshes and seeded inputs.
+
+Tolerances: FP64 path 1e-12 relative to the largest entry (round-off of
+reordered sums); mixed path (FP32 operator, FP64 state) 2e-5 relative for a
+single operator application."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 2e-5
+
+
+@pytest.fixture(scope="module")
+def env(oracle_mod):
+    import torch
+    from exwave_gb300 import build
+    build.build()
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    import exwave_gb300 as ew
+    return ew, oracle_mod, torch
+
+
+def make_case(ew, dim, n, ref, f, bids, hetero, seed):
+    m = ew.hypercube(dim, n, ref, f, boundary_ids=bids)
+    if hetero:
+        rng = np.random.default_rng(seed)
+        m.speed = rng.uniform(1.0, 4.0, m.n_cells)
+        m.density = rng.uniform(1.0, 3.0, m.n_cells)
+    return m
+
+
+CASES = [
+    # dim, k, intervals, refinements, transform, boundary ids, heterogeneous
+    (2, 1, 20, 0, 0.0, 2, False),
+    (2, 4, 16, 0, 0.0, 2, False),
+    (2, 3, 5, 2, 0.1, 2, False),
+    (2, 6, 5, 1, 0.0, [1, 2, 3, 1], True),
+    (2, 2, 6, 0, 0.15, [3, 3, 1, 2], True),
+    (2, 5, 4, 1, 0.1, [1, 1, 3, 3], True),
+    (2, 7, 3, 0, 0.0, 2, True),
+    (3, 1, 4, 0, 0.1, 2, False),
+    (3, 2, 4, 0, 0.0, [1, 2, 3, 1, 2, 3], True),
+    (3, 3, 3, 1, 0.1, [3, 1, 2, 2, 1, 3], True),
+    (3, 4, 5, 0, 0.1, 2, False),
+    (3, 5, 4, 0, 0.0, 2, True),
+    (3, 6, 3, 0, 0.05, [1, 1, 1, 1, 1, 2], True),
+    (3, 7, 3, 0, 0.05, 2, False),
+]
+
+
+def ids(c):
+    return "d%dk%d_n%d_r%d_f%g_%s" % (c[0], c[1], c[2], c[3], c[4], "het" if c[6] else "hom")
+
+
+@pytest.mark.parametrize("case", CASES, ids=ids)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_apply(env, case, precision):
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=k + 10 * dim)
+    op = ew.WaveEquationOperation(m, k, precision=precision)
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    rng = np.random.default_rng(1234 + k)
+    u = rng.standard_normal(o.n_dofs)
+    ref_out = o.apply(u)
+    src = torch.from_numpy(u).cuda()
+    dst = torch.zeros_like(src)
+    op.apply(src, dst)
+    op.synchronize()
+    got = dst.cpu().numpy()
+    err = np.abs(got - ref_out).max() / np.abs(ref_out).max()
+    assert err < (FP64_TOL if precision == "fp64" else MIXED_TOL), err
+
+
+@pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 3, 9, 10, 12)], ids=ids)
+def test_lsrk45_steps(env, case):
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=7)
+    op = ew.WaveEquationOperation(m, k, precision="fp64")
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    u0 = o.project_reference(2)
+    dt = o.time_step(0.3 / k ** 1.5)
+    a, b = u0.copy(), np.zeros_like(u0)
+    vn = torch.from_numpy(u0.copy()).cuda()
+    vnp = torch.zeros_like(vn)
+    for _ in range(3):
+        o.lsrk45_step(dt, a, b)
+        a, b = b, a
+        op.lsrk45_step(dt, vn, vnp)
+        vn, vnp = vnp, vn
+    op.synchronize()
+    err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
+    assert err < FP64_TOL, err
+
+
+@pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 5, 9, 10, 13)], ids=ids)
+@pytest.mark.parametrize("post", [False, True])
+def test_ader_step(env, case, post):
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=11)
+    op = ew.WaveEquationOperation(m, k, precision="fp64", use_ader_post=post)
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    o.set_ader_post(post)
+    u0 = o.project_reference(2)
+    dt = o.time_step(0.2 / k ** 1.5)
+    # apply_ader (reference sign: dst = -M^-1 A(T))
+    ref_dst = o.apply_ader(dt, u0)
+    src = torch.from_numpy(u0.copy()).cuda()
+    dst = torch.zeros_like(src)
+    op.apply_ader(src, dst, dt)
+    op.synchronize()
+    err = np.abs(dst.cpu().numpy() - ref_dst).max() / np.abs(ref_dst).max()
+    assert err < FP64_TOL, err
+    # two full steps
+    a, b = u0.copy(), np.zeros_like(u0)
+    vn = torch.from_numpy(u0.copy()).cuda()
+    vnp = torch.zeros_like(vn)
+    for _ in range(2):
+        o.ader_step(dt, a, b)
+        a, b = b, a
+        op.ader_step(dt, vn, vnp)
+        vn, vnp = vnp, vn
+    op.synchronize()
+    err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
+    assert err < FP64_TOL, err
+
+
+def test_rk_update_matches_reference_updater(env):
+    ew, oracle, torch = env
+    m = ew.hypercube(2, 4)
+    op = ew.WaveEquationOperation(m, 2)
+    rng = np.random.default_rng(5)
+    v1, v2, v3 = (rng.standard_normal(op.n_dofs) for _ in range(3))
+    for last in (0, 1):
+        a1, a2, a3 = v1.copy(), v2.copy(), v3.copy()
+        oracle.lib().ewo_rk_update(op.n_dofs, 0.3, -0.7, last, *(oracle._dp(x) for x in (a1, a2, a3)))
+        g1, g2, g3 = (torch.from_numpy(x.copy()).cuda() for x in (v1, v2, v3))
+        op.rk_update(0.3, -0.7, last, g1, g2, g3)
+        op.synchronize()
+        np.testing.assert_allclose(g2.cpu().numpy(), a2, rtol=1e-15, atol=1e-15)
+        np.testing.assert_allclose(g3.cpu().numpy(), a3, rtol=1e-15, atol=1e-15)
+
+
+def test_two_register_contract(env):
+    """vec_np receives the new state; vec_n is a register; equal pointers are
+    rejected (the in-place aliasing hazard of the fused update)."""
+    ew, oracle, torch = env
+    m = ew.hypercube(3, 3)
+    op = ew.WaveEquationOperation(m, 3)
+    u = op.project_membrane(*ew.reference_mode(3, 1))
+    with pytest.raises(Exception):
+        op.lsrk45_step(1e-3, u, u)
+    with pytest.raises(Exception):
+        op.ader_step(1e-3, u, u)
+
+
+def test_projection_and_errors_match_oracle(env):
+    ew, oracle, torch = env
+    m = ew.hypercube(3, 4, 0, 0.1)
+    o = oracle.Problem.from_mesh(3, 4, m.vertices, m.neighbors, m.speed, m.density)
+    op = ew.WaveEquationOperation(m, 4)
+    amps, kv = [1.0, 0.5], [[1, 1, 1], [2, 1, 3]]
+    u = op.project_membrane(amps, kv, 0.3)
+    ref = o.project_modes(amps, kv, 0.3)
+    np.testing.assert_allclose(u.cpu().numpy(), ref, rtol=0, atol=1e-14)
+    e_gpu = op.l2_errors(u * 1.01, amps, kv, 0.3)
+    e_ref = o.errors_modes(ref * 1.01, amps, kv, 0.3)
+    np.testing.assert_allclose(e_gpu, e_ref, rtol=1e-12)
