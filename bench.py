@@ -53,6 +53,13 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="membrane3d",
+                    choices=["membrane3d", "ader3d", "batch", "serve", "sweep"],
+                    help="membrane3d (default headline), ader3d (curved two-layer ADER), batch "
+                         "(512 independent solves), serve (continuous batching), sweep (degrees)")
+    ap.add_argument("--solves", type=int, default=512)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--time-limit", type=float, default=60.0)
     return ap.parse_args()
 
 
@@ -259,10 +266,178 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ader3d(args, torch):
+    """ADER of order k+1, 3-D k=4, 40^3 hexes on the curved mesh x_i += 0.03
+    prod_d sin(2 pi x_d), two layers split at z = 0.5 (c=1, rho=1 below; c=3,
+    rho=2 above), Gaussian pulse (width 0.05) at a seeded point of the lower
+    layer, p = 0 on the top face, rigid walls elsewhere; CFL 0.2."""
+    import numpy as np
+    import exwave_gb300 as ew
+    k, n = 4, (args.cells if args.cells != 64 else 40)
+    m = ew.hypercube(3, n, 0, 0.03, transform="sine_all", boundary_ids=[1, 1, 1, 1, 1, 2])
+    ew.layered_materials(m, 0.5, below=(1.0, 1.0), above=(3.0, 2.0))
+    rng = np.random.default_rng(2024)
+    x0 = [rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.15, 0.35)]
+    dt = ew.time_step_size(m, 0.2 / k ** 1.5)
+    out = {}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        op = ew.WaveEquationOperation(m, k, precision=prec)
+        u = op.project_gaussian(x0, 0.05)
+        v = torch.zeros_like(u)
+        steps = args.steps if prec == "mixed" else max(2, args.steps // 4)
+        for _ in range(args.warmup):
+            op.ader_step(dt, u, v)
+            u, v = v, u
+        stream = torch.cuda.current_stream()
+        op.set_stream(stream)
+        l0 = op.kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            op.ader_step(dt, u, v)
+            u, v = v, u
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {"value": op.n_dofs * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "gpu_launches": op.kernel_launches() - l0}
+        op.synchronize()
+        states[prec] = (op, u, steps)
+    # same number of steps on both paths for the comparison
+    n_cmp = states["fp64"][2] + args.warmup
+    opm = ew.WaveEquationOperation(m, k, precision="mixed")
+    um = opm.project_gaussian(x0, 0.05)
+    vm = torch.zeros_like(um)
+    op64 = ew.WaveEquationOperation(m, k, precision="fp64")
+    u64 = op64.project_gaussian(x0, 0.05)
+    v64 = torch.zeros_like(u64)
+    for _ in range(n_cmp):
+        opm.ader_step(dt, um, vm)
+        um, vm = vm, um
+        op64.ader_step(dt, u64, v64)
+        u64, v64 = v64, u64
+    diff = op64.l2_difference(um, u64)
+    ref = op64.l2_difference(u64, torch.zeros_like(u64))
+    return {"metric": "DoF-updates/s (ADER: 1 per DoF and step)", "value": out["mixed"]["value"],
+            "unit": "DoF-updates/s", "ms_per_step": out["mixed"]["ms_per_step"],
+            "fp64": out["fp64"], "gpu_launches": out["mixed"]["gpu_launches"],
+            "mixed_vs_fp64_rel_l2_p": diff[0] / ref[0], "mixed_vs_fp64_rel_l2_u":
+            diff[1] / max(ref[1], 1e-300), "compare_steps": n_cmp,
+            "config": {"workload": "ADER k=4 3-D 40^3 curved two-layer Gaussian pulse",
+                       "n_dofs": opm.n_dofs, "dt": dt, "x0": x0}}
+
+
+def batch_workload(args, torch):
+    """Batch of independent 3-D solves drawn from a seed (degree uniform in
+    {3..7}, n^3 cells n in [8,32], c ~ U[1,4], rho ~ U[1,3], Ricker source
+    f0 ~ U[2,8], 8 receivers), all resident; K batch steps timed (every solve
+    advances one LSRK45 step per batch step); compared with running a sample
+    of the same solves one after another."""
+    import numpy as np
+    from exwave_gb300 import serve
+    from exwave_gb300.batch import Batch
+    reqs = serve.draw_requests(args.solves, rate=0.0, seed=7, end_time=(1.0, 1.0))
+    solves = [r.make_solve() for r in reqs]
+    free, total = torch.cuda.mem_get_info()
+    b = Batch(precision=args.precision, hbm_budget_bytes=int(free * 0.85), max_solves=len(solves) + 8)
+    for s in solves:
+        b.add(s)
+    dofs = sum(r.dofs() for r in reqs)
+    stream = torch.cuda.current_stream()
+    b.set_stream(stream)
+    b.step(args.warmup)
+    b.synchronize()
+    l0 = b.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(args.steps)
+    e1.record(stream)
+    b.synchronize()
+    ms = e0.elapsed_time(e1)
+    batched = dofs * 5 * args.steps / (ms / 1e3)
+    launches = b.kernel_launches() - l0
+    b.close()
+    # sequential: a seeded sample of the same solves, each alone
+    rng = np.random.default_rng(1)
+    idx = rng.choice(len(solves), size=min(16, len(solves)), replace=False)
+    seq_t, seq_d = 0.0, 0
+    for i in idx:
+        one = Batch(precision=args.precision, hbm_budget_bytes=4 << 30, max_solves=2)
+        one.add(solves[i])
+        one.set_stream(stream)
+        one.step(1)
+        one.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        one.step(args.steps)
+        f1.record(stream)
+        one.synchronize()
+        seq_t += f0.elapsed_time(f1) / 1e3
+        seq_d += reqs[i].dofs() * 5 * args.steps
+        one.close()
+    sequential = seq_d / seq_t
+    return {"metric": "DoF-updates/s (aggregate)", "value": batched, "unit": "DoF-updates/s",
+            "ms_per_step": ms / args.steps, "gpu_launches": int(launches),
+            "sequential_value": sequential, "batched_over_sequential": batched / sequential,
+            "config": {"workload": "batch of %d 3-D solves (k 3..7, n 8..32, Ricker, 8 receivers)"
+                                   % len(solves), "total_dofs": dofs, "precision": args.precision,
+                       "sequential_sample": len(idx)}}
+
+
+def serve_workload(args, torch):
+    from exwave_gb300 import serve
+    reqs = serve.draw_requests(args.solves if args.solves != 512 else 20000, rate=args.rate,
+                               seed=11)
+    srv = serve.Server(precision=args.precision, hbm_budget_bytes=150 << 30, steps_per_tick=4)
+    stats = srv.run(reqs, time_limit=args.time_limit)
+    return {"metric": "solves/s", "value": stats["solves_per_s"], "unit": "solves/s",
+            "latency_p50_s": stats["latency_p50_s"], "latency_p99_s": stats["latency_p99_s"],
+            "stats": stats, "config": {"workload": "serving, Poisson %.0f/s, T ~ U[0.2,2], "
+                                                   "150 GB budget, %d requests, %g s limit"
+                                                   % (args.rate, len(reqs), args.time_limit)}}
+
+
+def sweep_workload(args, torch):
+    import exwave_gb300 as ew
+    rows = []
+    for k, n in ((2, 128), (3, 96), (4, 77), (5, 64), (6, 55), (7, 48)):
+        m, dt = build_problem(n, k)
+        row = {"degree": k, "cells": n}
+        for prec in ("mixed", "fp64"):
+            op = ew.WaveEquationOperation(m, k, precision=prec)
+            steps = args.steps if prec == "mixed" else max(2, args.steps // 4)
+            ms, _, errs, _ = time_steps(op, dt, steps, min(args.warmup, 3), torch, lambda: None)
+            row[prec] = {"value": op.n_dofs * STAGES * steps / (ms / 1e3),
+                         "ms_per_step": ms / steps, "l2_p": errs[0],
+                         "gbs": BYTES_PER_DOF_STEP[prec] * op.n_dofs / (ms / steps / 1e3) / 1e9}
+            row["n_dofs"] = op.n_dofs
+            op.close()
+        rows.append(row)
+    return {"metric": "DoF-updates/s per degree", "rows": rows,
+            "config": {"workload": "3-D membrane degree sweep at ~226M DoFs"}}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "membrane3d":
+        import torch
+        from exwave_gb300 import build
+        build.build()
+        fn = {"ader3d": ader3d, "batch": batch_workload, "serve": serve_workload,
+              "sweep": sweep_workload}[args.workload]
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            res = fn(args, torch)
+        res["clocks"] = clk.summary()
+        res["n_gpus"] = 1
+        print(json.dumps(res), flush=True)
         return
     import torch
     ws, rank, local = dist_info()

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -14,11 +15,12 @@
 
 #include "../../include/exwave_gb300.h"
 #include "ew_basis.h"
+#include "ew_internal.h"
 #include "ew_launch.h"
 
 namespace ew {
-namespace {
 
+namespace {
 KernelTable g_tables[2][9];
 std::once_flag g_tables_once;
 
@@ -38,19 +40,27 @@ void init_tables() {
   kernel_table_d3_7(g_tables[1][7]);
   kernel_table_d3_8(g_tables[1][8]);
 }
+}  // namespace
 
+const KernelTable& kernel_table(int dim, int np) {
+  std::call_once(g_tables_once, init_tables);
+  return g_tables[dim - 2][np];
+}
+
+cudaError_t upload_cart_constants(int dim, int np) {
+  GaussRule g = gauss_rule(np);
+  std::vector<double> D(np * np), L0(np), L1(np);
+  for (int i = 0; i < np; ++i)
+    for (int j = 0; j < np; ++j) D[i * np + j] = lagrange_deriv(g.x, j, g.x[i]);
+  for (int j = 0; j < np; ++j) {
+    L0[j] = lagrange(g.x, j, 0.0);
+    L1[j] = lagrange(g.x, j, 1.0);
+  }
+  return kernel_table(dim, np).set_constants(g.w.data(), D.data(), L0.data(), L1.data());
+}
+
+namespace {
 thread_local std::string g_create_error;
-
-// LowStorageRK45Reg2 coefficients (time_integrators.cc:243-252)
-constexpr double kA21 = 970286171893. / 4311952581923.;
-constexpr double kA32 = 6584761158862. / 12103376702013.;
-constexpr double kA43 = 2251764453980. / 15575788980749.;
-constexpr double kA54 = 26877169314380. / 34165994151039.;
-constexpr double kB1 = 1153189308089. / 22510343858157.;
-constexpr double kB2 = 1772645290293. / 4653164025191.;
-constexpr double kB3 = -1672844663538. / 4480602732383.;
-constexpr double kB4 = 2114624349019. / 3568978502595.;
-constexpr double kB5 = 5198255086312. / 14908931495163.;
 
 constexpr int kMaxModes = 8;
 struct Modes {
@@ -292,6 +302,10 @@ struct ew_ctx {
   int n_work_stage = 0;
   ew::WorkItem* d_work_ck = nullptr;
   int n_work_ck = 0;
+  void* d_cellc = nullptr;  // Cartesian kernel per-cell constants
+  ew::WorkItem* d_work_cart = nullptr;
+  int n_work_cart = 0;
+  int cb_cart = 1;
   int grid_stage[ew::N_STAGE_VARIANTS] = {0, 0, 0};
   int grid_ck = 0;
   int* d_err = nullptr;
@@ -342,7 +356,7 @@ void free_ctx(ew_ctx* c) {
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
-                  c->d_work_stage, c->d_work_ck, c->d_err, c->d_tmp64, c->d_x32[0],
+                  c->d_work_stage, c->d_work_ck, c->d_work_cart, c->d_cellc, c->d_err, c->d_tmp64, c->d_x32[0],
                   c->d_x32[1], c->d_acc, c->d_l2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -352,7 +366,7 @@ void free_ctx(ew_ctx* c) {
 
 // Checks of the mesh description (the reference relies on deal.II's
 // Triangulation for these invariants).
-int validate_mesh(const ew_mesh_desc* m, bool* cartesian) {
+int validate_mesh_impl(const ew_mesh_desc* m, bool* cartesian) {
   if (!m) return fail(nullptr, EW_ERR_INVALID, "mesh is NULL");
   if (m->dim != 2 && m->dim != 3) return fail(nullptr, EW_ERR_INVALID, "dim must be 2 or 3");
   if (m->degree < 1 || m->degree > EW_MAX_DEGREE)
@@ -410,6 +424,16 @@ int validate_mesh(const ew_mesh_desc* m, bool* cartesian) {
   return EW_OK;
 }
 
+}  // namespace
+
+int ew::validate_mesh(const ew_mesh_desc* m, bool* cartesian, std::string* err) {
+  const int rc = validate_mesh_impl(m, cartesian);
+  if (rc && err) *err = ew::g_create_error;
+  return rc;
+}
+
+namespace {
+
 template <typename Real>
 std::vector<Real> to_real_vec(const std::vector<double>& v) {
   return std::vector<Real>(v.begin(), v.end());
@@ -449,6 +473,8 @@ ew::LaunchArgs base_args(ew_ctx* c, bool ck) {
   a.single.nbr = c->d_nbr;
   a.single.geo = c->d_geo;
   a.single.mat = c->d_mat;
+  a.single.cellc = c->d_cellc;
+  a.single.src_cell = -1;
   a.single.n_cells = c->n_cells;
   a.single.bf = 1.0f;
   a.solves = nullptr;
@@ -479,8 +505,28 @@ int launch_stage(ew_ctx* c, int variant, const double* A, const void* X, void* X
   split(f1 + f2, &a.single.fb_hi, &a.single.fb_lo);
   a.single.bf = bf;
   a.single.mode = mode;
-  const ew::KernelEntry& k = c->kt->stage[variant][c->cart ? 1 : 0];
-  cudaError_t e = k.launch(a, c->grid_stage[variant], c->stream);
+  cudaError_t e;
+  if (c->cart) {
+    // line kernel: stage X unless it is the accumulator itself (first LSRK
+    // stage), stage A in the RK modes; bulk copies need 16-byte alignment
+    const size_t in_sz = variant == ew::STAGE_MIX_IN32 ? 4 : 8;
+    const int sa = mode != ew::MODE_APPLY ? 1 : 0;
+    const int sx = (sa && static_cast<const void*>(A) == X && in_sz == 8) ? 0 : 1;
+    const size_t cell_elems = (size_t)c->F * c->N;
+    const bool tma = (cell_elems * in_sz) % 16 == 0 && (cell_elems * 8) % 16 == 0 &&
+                     (reinterpret_cast<uintptr_t>(X) % 16) == 0 &&
+                     (reinterpret_cast<uintptr_t>(A) % 16) == 0;
+    a.work = c->d_work_cart;
+    a.n_work = c->n_work_cart;
+    a.cells_per_block = c->cb_cart;
+    const ew::CartEntry& k = c->kt->cart[variant];
+    const int occ = std::max(1, k.occupancy(c->cb_cart, sx, sa));
+    const int grid = std::max(1, std::min(c->n_work_cart, occ * c->num_sms));
+    e = k.launch(a, sx, sa, tma ? 1 : 0, grid, c->stream);
+  } else {
+    const ew::KernelEntry& k = c->kt->stage[variant][0];
+    e = k.launch(a, c->grid_stage[variant], c->stream);
+  }
   ++c->launches;
   if (e != cudaSuccess) return cuda_fail(c, e, "stage kernel launch");
   return EW_OK;
@@ -510,9 +556,8 @@ const char* ew_last_error(const ew_ctx* ctx) {
 int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out) {
   if (!out) return fail(nullptr, EW_ERR_INVALID, "ctx output pointer is NULL");
   *out = nullptr;
-  std::call_once(ew::g_tables_once, ew::init_tables);
   bool cart = false;
-  int rc = validate_mesh(mesh, &cart);
+  int rc = validate_mesh_impl(mesh, &cart);
   if (rc) return rc;
   ew_options opt;
   std::memset(&opt, 0, sizeof(opt));
@@ -549,7 +594,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   c->mixed = opt.precision == EW_PREC_MIXED;
   c->cart = cart;
   c->post = opt.use_ader_post != 0;
-  c->kt = &ew::g_tables[c->dim - 2][c->np];
+  c->kt = &ew::kernel_table(c->dim, c->np);
   const int dim = c->dim, nv = 1 << dim;
 
   auto bail = [&](int code) {
@@ -568,12 +613,39 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     else
       std::copy(V, V + nv * dim, geo.begin() + i * nv * dim);
   }
-  std::vector<double> mat((size_t)c->n_cells * 2);
+  // per cell: rho, c, tau = 1/(c rho), 1/rho
+  std::vector<double> mat((size_t)c->n_cells * 4);
   for (int64_t i = 0; i < c->n_cells; ++i) {
-    mat[2 * i] = mesh->density[i];
-    mat[2 * i + 1] = mesh->speed[i];
+    mat[4 * i] = mesh->density[i];
+    mat[4 * i + 1] = mesh->speed[i];
+    mat[4 * i + 2] = 1.0 / (mesh->speed[i] * mesh->density[i]);
+    mat[4 * i + 3] = 1.0 / mesh->density[i];
   }
   std::vector<double> basis = ew::basis_table(c->np);
+  // Cartesian kernel constants per cell: 1/rho, rho c^2, tau, 1/tau,
+  // 1/h_e (3 slots), per face (tau of the neighbour, 1/(tau + tau_nb))
+  std::vector<double> cellc;
+  if (cart) {
+    const int K = 19;
+    cellc.assign((size_t)c->n_cells * K, 0.0);
+    for (int64_t i = 0; i < c->n_cells; ++i) {
+      double* k = &cellc[(size_t)i * K];
+      const double rho = mesh->density[i], sp = mesh->speed[i];
+      const double tau = 1.0 / (sp * rho);
+      k[0] = 1.0 / rho;
+      k[1] = rho * sp * sp;
+      k[2] = tau;
+      k[3] = sp * rho;
+      for (int e = 0; e < dim; ++e) k[4 + e] = 1.0 / geo[i * dim + e];
+      for (int f = 0; f < 2 * dim; ++f) {
+        const int32_t nb = mesh->neighbors[i * 2 * dim + f];
+        if (nb < 0) continue;
+        const double tm = 1.0 / (mesh->speed[nb] * mesh->density[nb]);
+        k[7 + 2 * f] = tm;
+        k[8 + 2 * f] = 1.0 / (tau + tm);
+      }
+    }
+  }
   const size_t rsz = c->mixed ? sizeof(float) : sizeof(double);
   if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_geo), geo.size() * rsz)) ||
       (rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_mat), mat.size() * rsz)) ||
@@ -594,6 +666,16 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
         (rc = upload(c, c->d_mat, mat.data(), mat.size() * 8)) ||
         (rc = upload(c, c->d_basis, basis.data(), basis.size() * 8)))
       return bail(rc);
+  }
+  if (cart) {
+    if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_cellc), cellc.size() * rsz))) return bail(rc);
+    if (c->mixed) {
+      auto f = to_real_vec<float>(cellc);
+      rc = upload(c, c->d_cellc, f.data(), f.size() * 4);
+    } else {
+      rc = upload(c, c->d_cellc, cellc.data(), cellc.size() * 8);
+    }
+    if (rc) return bail(rc);
   }
   if ((rc = upload(c, c->d_nbr, mesh->neighbors, (size_t)c->n_cells * 2 * dim * 4)) ||
       (rc = upload(c, c->d_verts, mesh->vertices, (size_t)c->n_cells * nv * dim * 8)))
@@ -616,6 +698,9 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   if (cudaMemset(c->d_err, 0, 4 * sizeof(int)) != cudaSuccess)
     return bail(fail(c, EW_ERR_CUDA, "cudaMemset"));
 
+  // even-odd 1D constants of the Cartesian kernel, for this device
+  ce = ew::upload_cart_constants(c->dim, c->np);
+  if (ce != cudaSuccess) return bail(cuda_fail(c, ce, "constant upload"));
   // work lists and persistent grid sizes
   c->cb_stage = default_cb(c->N, opt.cells_per_block);
   c->cb_ck = c->cb_stage;
@@ -623,8 +708,16 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   while (c->cb_ck > 1 &&
          c->kt->ck[ck_var][cart][c->post].smem(c->cb_ck) > 200 * 1024)
     --c->cb_ck;
+  if (cart) {
+    const int lines = c->kt->lines;
+    c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block : std::max(1, 256 / lines);
+    c->cb_cart = std::max(1, std::min(c->cb_cart, 256 / lines));
+    const int v = c->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
+    while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1, 1) > 110 * 1024) --c->cb_cart;
+  }
   if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
-      (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)))
+      (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)) ||
+      (cart && (rc = build_work(c, c->cb_cart, &c->d_work_cart, &c->n_work_cart))))
     return bail(rc);
   for (int v = 0; v < ew::N_STAGE_VARIANTS; ++v) {
     const int occ = c->kt->stage[v][cart].occupancy(c->cb_stage);
@@ -864,6 +957,7 @@ int ew_synchronize(ew_ctx* ctx) {
     if (flags & ew::ERR_BAD_NEIGHBOR) m += ": neighbor index out of range";
     if (flags & ew::ERR_BAD_BOUNDARY_ID) m += ": invalid boundary id";
     if (flags & ew::ERR_BAD_LAUNCH) m += ": launch shape mismatch";
+    if (flags & 8) m += ": wait for a bulk copy timed out";
     cudaMemset(ctx->d_err, 0, sizeof(int));
     return fail(ctx, EW_ERR_DEVICE, m);
   }

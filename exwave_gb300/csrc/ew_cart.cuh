@@ -1,0 +1,560 @@
+// ew_cart.cuh -- stage kernel for Cartesian (axis-aligned box) cells.
+//
+// On a Cartesian cell the Jacobian is diag(h), so in direction e only the
+// velocity component u_e and the pressure interact: the cell term gives
+// k_{u_e} = -rho^{-1}/h_e d_e p and a pressure part rho c^2/h_e (D^T w u_e)/w,
+// and the faces normal to e lift only u_e and p.  The kernel therefore runs
+// one thread per (cell, direction, line): it holds the line of u_e and p in
+// registers, evaluates both face traces, the neighbours' traces, the two
+// upwind fluxes, the derivative and weighted-transpose contractions with
+// even-odd splitting (half the multiply-adds), and finishes the update of
+// u_e on that line; pressure contributions of the directions meet in shared
+// memory and are finished by one thread per point.
+//
+// Input staging: each work item's contiguous block of cells (stage input X
+// and accumulator A) is copied into shared memory with one 1-D bulk copy
+// (cp.async.bulk, TMA engine) per array, completed on an mbarrier; the
+// copies of the next work item are issued before the current one is
+// processed (double buffering).  Waits are bounded; on time-out the kernel
+// raises ERR_WAIT_TIMEOUT and skips the item.
+#pragma once
+
+#include <cstring>
+
+#include "ew_kernels.cuh"
+
+namespace ew {
+
+constexpr int ERR_WAIT_TIMEOUT = 8;
+
+// Even-odd form of an NP x NP matrix M with M[n-1-i][n-1-j] = -M[i][j]:
+// for i < H = NP/2, a_i = sum_j P_ij e_j (+ mid_col_i x_m), b_i = sum_j Q_ij o_j,
+// y_i = a_i + b_i, y_{n-1-i} = b_i - a_i, and for odd NP y_m = sum_j mid_row_j o_j,
+// with e_j = x_j + x_{n-1-j}, o_j = x_j - x_{n-1-j}.
+template <typename Real>
+struct EoMat {
+  Real P[4][4], Q[4][4];
+  Real mid_row[4], mid_col[4];
+};
+
+template <typename Real>
+struct CartBasis {
+  EoMat<Real> D;   // D[i][j] = l_j'(x_i)
+  EoMat<Real> Dt;  // Dt[i][a] = D[a][i] w_a / w_i
+  Real Ls[4], La[4], Lmid;  // traces: t0 = s + a, t1 = s - a
+  Real Ws[4], Wa[4], Wmid;  // lifts with l_j(s)/w_j
+  Real L[2][8];             // l_j(0), l_j(1) (neighbour traces)
+};
+
+// Host-side construction from the 1D Gauss data.
+inline void make_eo(const double* M, int NP, EoMat<double>& E) {
+  const int H = NP / 2;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) E.P[i][j] = E.Q[i][j] = 0.0;
+  for (int i = 0; i < 4; ++i) E.mid_row[i] = E.mid_col[i] = 0.0;
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < H; ++j) {
+      E.P[i][j] = 0.5 * (M[i * NP + j] + M[i * NP + NP - 1 - j]);
+      E.Q[i][j] = 0.5 * (M[i * NP + j] - M[i * NP + NP - 1 - j]);
+    }
+  if (NP % 2) {
+    const int m = NP / 2;
+    for (int j = 0; j < H; ++j) E.mid_row[j] = M[m * NP + j];
+    for (int i = 0; i < H; ++i) E.mid_col[i] = M[i * NP + m];
+  }
+}
+
+template <int NP, typename Real>
+__device__ __forceinline__ void eo_apply(const EoMat<Real>& M, const Real* e, const Real* o,
+                                         Real xm, Real* a, Real* b) {
+  constexpr int H = NP / 2;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    Real s = Real(0), t = Real(0);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      s += M.P[i][j] * e[j];
+      t += M.Q[i][j] * o[j];
+    }
+    if constexpr (NP % 2 == 1) s += M.mid_col[i] * xm;
+    a[i] = s;
+    b[i] = t;
+  }
+  if constexpr (NP % 2 == 1) {
+    Real s = Real(0);
+#pragma unroll
+    for (int j = 0; j < H; ++j) s += M.mid_row[j] * o[j];
+    a[H] = s;  // middle output (no pair)
+  }
+}
+
+// One copy per instantiation unit (each unit serves one NP); filled from
+// the host by set_cart_constants for the current device.
+namespace {
+__constant__ CartBasis<float> c_cart_f;
+__constant__ CartBasis<double> c_cart_d;
+}  // namespace
+template <typename Real>
+struct CartConst;
+template <>
+struct CartConst<float> {
+  static __device__ __forceinline__ const CartBasis<float>& get() { return c_cart_f; }
+};
+template <>
+struct CartConst<double> {
+  static __device__ __forceinline__ const CartBasis<double>& get() { return c_cart_d; }
+};
+
+// Host: even-odd constants from the 1D Gauss data of NP points.
+inline CartBasis<double> make_cart_basis(int NP, const double* w, const double* D,
+                                         const double* L0, const double* L1) {
+  CartBasis<double> c;
+  std::memset(&c, 0, sizeof(c));
+  make_eo(D, NP, c.D);
+  double Dt[64];
+  for (int i = 0; i < NP; ++i)
+    for (int a = 0; a < NP; ++a) Dt[i * NP + a] = D[a * NP + i] * w[a] / w[i];
+  make_eo(Dt, NP, c.Dt);
+  const int H = NP / 2;
+  for (int j = 0; j < H; ++j) {
+    c.Ls[j] = 0.5 * (L0[j] + L0[NP - 1 - j]);
+    c.La[j] = 0.5 * (L0[j] - L0[NP - 1 - j]);
+    const double a = L0[j] / w[j], b = L0[NP - 1 - j] / w[NP - 1 - j];
+    c.Ws[j] = 0.5 * (a + b);
+    c.Wa[j] = 0.5 * (a - b);
+  }
+  if (NP % 2) {
+    c.Lmid = L0[NP / 2];
+    c.Wmid = L0[NP / 2] / w[NP / 2];
+  }
+  for (int j = 0; j < NP; ++j) {
+    c.L[0][j] = L0[j];
+    c.L[1][j] = L1[j];
+  }
+  return c;
+}
+
+template <typename Real>
+inline CartBasis<Real> cast_basis(const CartBasis<double>& d) {
+  CartBasis<Real> r;
+  const double* src = reinterpret_cast<const double*>(&d);
+  Real* dst = reinterpret_cast<Real*>(&r);
+  for (size_t i = 0; i < sizeof(d) / sizeof(double); ++i) dst[i] = static_cast<Real>(src[i]);
+  return r;
+}
+
+// ---------------------------------------------------------------- mbarrier / bulk copy
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Per-cell constants kept in shared memory: rho^{-1}, rho c^2, tau = 1/(c rho),
+// 1/tau, 1/h_e (3), and per face (tau of the neighbour, 1/(tau + tau_nb)).
+constexpr int kCellConsts = 4 + 3 + 6 * 2;
+
+// Shared-memory layout of the Cartesian kernel (bytes).
+template <int DIM, int NP, typename Real, typename InT>
+struct CartSmem {
+  static constexpr int N = ipow_c(NP, DIM);
+  static constexpr int F = DIM + 1;
+  size_t bar, X, A, Kp, cell, end;
+  int xbytes, abytes;  // per buffer
+  __host__ __device__ CartSmem(int CB, bool stage_x, bool stage_a) {
+    bar = 0;  // 4 mbarriers (X and A, double buffered)
+    X = 64;
+    xbytes = stage_x ? CB * F * N * (int)sizeof(InT) : 0;
+    A = X + 2 * (size_t)((xbytes + 127) & ~127);
+    abytes = stage_a ? CB * F * N * (int)sizeof(double) : 0;
+    Kp = A + 2 * (size_t)((abytes + 127) & ~127);
+    cell = Kp + (size_t)DIM * CB * N * sizeof(Real);
+    end = cell + (size_t)CB * kCellConsts * sizeof(Real);
+    end = (end + 127) & ~(size_t)127;
+  }
+};
+
+// Stage update of one value: RK_MID gives the next stage input (xn) and
+// accumulator (an), RK_LAST the accumulator.  FP64 path: the reference's
+// RKVectorUpdater arithmetic; mixed path: FP32 increment added to the FP64
+// accumulator, conversions on the integer pipe.
+template <typename Real, typename OutT>
+__device__ __forceinline__ void update_point(const SolveDesc& sd, int mode, double a, Real k,
+                                             OutT& xn, double& an) {
+  if constexpr (sizeof(Real) == 8) {
+    if (mode == MODE_RK_MID) {
+      const double x = a + sd.f1 * k;
+      xn = static_cast<OutT>(x);
+      an = x + sd.f2 * k;
+    } else {
+      xn = OutT(0);
+      an = a + sd.f1 * k;
+    }
+  } else {
+    if (mode == MODE_RK_MID) {
+      xn = static_cast<OutT>(fmaf(sd.f1f, k, f64_to_f32(a)));
+      an = a + f32_to_f64(fmaf(sd.fb_hi, k, sd.fb_lo * k));
+    } else {
+      xn = OutT(0);
+      an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
+    }
+  }
+}
+
+__device__ __forceinline__ void store2(float* p, float a, float b) {
+  *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+__device__ __forceinline__ void store2(double* p, double a, double b) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+}
+
+struct CartArgs {
+  LaunchArgs la;
+  int32_t stage_x;  // X staged in shared memory (else read from A's buffer: X == A)
+  int32_t stage_a;  // A staged (RK modes)
+  int32_t tma;      // bulk copies usable (alignment checked on the host)
+};
+
+template <int DIM, int NP, typename Real, typename InT, typename OutT>
+__global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
+  constexpr int N = ipow_c(NP, DIM);
+  constexpr int F = DIM + 1;
+  constexpr int NL = ipow_c(NP, DIM - 1);
+  constexpr int H = NP / 2;
+  const LaunchArgs& La = ca.la;
+  const int CB = La.cells_per_block;
+  extern __shared__ __align__(128) unsigned char smem_cart[];
+  const CartSmem<DIM, NP, Real, InT> lay(CB, ca.stage_x != 0, ca.stage_a != 0);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_cart + lay.bar);
+  const size_t xstride = (size_t)((lay.xbytes + 127) & ~127);
+  const size_t astride = (size_t)((lay.abytes + 127) & ~127);
+  Real* sKp = reinterpret_cast<Real*>(smem_cart + lay.Kp);
+  Real* sCell = reinterpret_cast<Real*>(smem_cart + lay.cell);
+  if ((int)blockDim.x != CB * DIM * NL) {
+    if (threadIdx.x == 0) atomicOr(La.err, ERR_BAD_LAUNCH);
+    return;
+  }
+  const CartBasis<Real>& B = CartConst<Real>::get();
+  const bool stage_x = ca.stage_x != 0, stage_a = ca.stage_a != 0;
+
+  // issue the copies of work item w into buffer b
+  auto issue = [&](int w, int b) {
+    const WorkItem wi = La.work[w];
+    const SolveDesc& sd = La.solves ? La.solves[wi.solve] : La.single;
+    const size_t c0 = (size_t)wi.cell_begin * F * N;
+    const uint32_t nx = (uint32_t)(wi.n_cells * F * N * sizeof(InT));
+    const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
+    uint32_t tx = 0;
+    if (stage_x) tx += nx;
+    if (stage_a) tx += na;
+    mbar_expect_tx(&bars[b], tx);
+    if (stage_x) bulk_g2s(smem_cart + lay.X + b * xstride, static_cast<const InT*>(sd.X) + c0, nx, &bars[b]);
+    if (stage_a) bulk_g2s(smem_cart + lay.A + b * astride, sd.A + c0, na, &bars[b]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (ca.tma && threadIdx.x == 0 && (int)blockIdx.x < La.n_work) issue(blockIdx.x, 0);
+
+  uint32_t phase = 0;  // bit b: parity of the next wait on buffer b
+  int it = 0;
+  for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
+    const int b = it & 1;
+    const WorkItem wi = La.work[w];
+    const SolveDesc& sd = La.solves ? La.solves[wi.solve] : La.single;
+    const int nc = wi.n_cells;
+    InT* sX = reinterpret_cast<InT*>(smem_cart + lay.X + b * xstride);
+    double* sA = reinterpret_cast<double*>(smem_cart + lay.A + b * astride);
+    // per-cell constants (prepared on the host, see ew_create)
+    {
+      const Real* gc = static_cast<const Real*>(sd.cellc) + (size_t)wi.cell_begin * kCellConsts;
+      for (int i = threadIdx.x; i < nc * kCellConsts; i += blockDim.x) sCell[i] = load_nc(gc + i);
+    }
+    // line task of this thread and the traces of its non-local neighbours
+    // (read from L2 while the bulk copies are in flight)
+    const int task = threadIdx.x;
+    const int tcl = task / (DIM * NL);
+    const int te = (task - tcl * DIM * NL) / NL;
+    const int tt = task - tcl * DIM * NL - te * NL;
+    const bool tactive = tcl < nc;
+    int tbase = 0;
+    {
+      int ti[3] = {0, 0, 0};
+      tbase = face_base<DIM, NP>(te, tt, ti);
+    }
+    const int tstr = dir_stride(te, NP);
+    int nbs[2] = {-EW_BC_HARD_WALL_ID, -EW_BC_HARD_WALL_ID};
+    Real nvu[2] = {Real(0), Real(0)}, nvp[2] = {Real(0), Real(0)};
+    if (tactive) {
+      const int cell = wi.cell_begin + tcl;
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        int nb = sd.nbr[(size_t)cell * 2 * DIM + 2 * te + s];
+        if (nb >= sd.n_cells) {
+          atomicOr(La.err, ERR_BAD_NEIGHBOR);
+          nb = cell;
+        }
+        nbs[s] = nb;
+        const int nl = nb - wi.cell_begin;
+        if (nb >= 0 && !(nl >= 0 && nl < nc)) {
+          const InT* xn = static_cast<const InT*>(sd.X) + (size_t)nb * F * N;
+          Real vu = Real(0), vp = Real(0);
+#pragma unroll
+          for (int j = 0; j < NP; ++j) {
+            const Real l = B.L[1 - s][j];
+            vu += l * to_real<Real>(load_nc(xn + te * N + tbase + j * tstr));
+            vp += l * to_real<Real>(load_nc(xn + DIM * N + tbase + j * tstr));
+          }
+          nvu[s] = vu;
+          nvp[s] = vp;
+        }
+      }
+    }
+    if (ca.tma) {
+      // prefetch the next item into the other buffer (its previous contents
+      // were consumed before the end-of-item barrier of the last iteration)
+      if (threadIdx.x == 0 && w + (int)gridDim.x < La.n_work) {
+        fence_proxy_async();
+        issue(w + gridDim.x, b ^ 1);
+      }
+      const bool ok = mbar_wait(&bars[b], (phase >> b) & 1u);
+      phase ^= (1u << b);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(La.err, ERR_WAIT_TIMEOUT);
+        continue;
+      }
+    } else {
+      const size_t c0 = (size_t)wi.cell_begin * F * N;
+      if (stage_x) {
+        const InT* gx = static_cast<const InT*>(sd.X) + c0;
+        for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sX[i] = gx[i];
+      }
+      if (stage_a) {
+        const double* ga = sd.A + c0;
+        for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sA[i] = ga[i];
+      }
+    }
+    __syncthreads();
+
+    // ---------------------------------------------------------- line phase
+    // stage input values as Real, from the X buffer or (X == A) the A buffer
+    auto xval = [&](int idx) -> Real {
+      if (stage_x) return to_real<Real>(sX[idx]);
+      return to_real<Real>(sA[idx]);
+    };
+    const Real bf = static_cast<Real>(sd.bf);
+    {
+      const int cl = tcl, e = te, base = tbase, str = tstr;
+      if (tactive) {
+        const Real* cst = sCell + cl * kCellConsts;
+        const Real rho_inv = cst[0], rc2 = cst[1], tau_p = cst[2], itau = cst[3], ih = cst[4 + e];
+        const int xo = cl * F * N;
+        Real xu[NP], xp[NP];
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          xu[j] = xval(xo + e * N + base + j * str);
+          xp[j] = xval(xo + DIM * N + base + j * str);
+        }
+        Real eu[4], ou[4], ep[4], op[4];
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+          eu[j] = xu[j] + xu[NP - 1 - j];
+          ou[j] = xu[j] - xu[NP - 1 - j];
+          ep[j] = xp[j] + xp[NP - 1 - j];
+          op[j] = xp[j] - xp[NP - 1 - j];
+        }
+        const Real um = (NP % 2) ? xu[NP / 2] : Real(0);
+        const Real pm = (NP % 2) ? xp[NP / 2] : Real(0);
+        // own traces at x_e = 0 (side 0) and x_e = 1 (side 1)
+        Real su = (NP % 2) ? B.Lmid * um : Real(0), au = Real(0);
+        Real sp = (NP % 2) ? B.Lmid * pm : Real(0), ap = Real(0);
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+          su += B.Ls[j] * eu[j];
+          au += B.La[j] * ou[j];
+          sp += B.Ls[j] * ep[j];
+          ap += B.La[j] * op[j];
+        }
+        const Real tu[2] = {su + au, su - au};
+        const Real tp[2] = {sp + ap, sp - ap};
+        // fluxes at both ends (without the face JxW)
+        Real Fu[2], Fp[2];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const Real nrm = s ? Real(1) : Real(-1);
+          const Real un_p = nrm * tu[s];
+          const int nb = nbs[s];
+          Real lambda;
+          if (nb >= 0) {
+            const int nl = nb - wi.cell_begin;
+            Real vu = nvu[s], vp = nvp[s];
+            if (nl >= 0 && nl < nc) {
+              // neighbour in this block: its trace on the opposite face, l_j(1-s)
+              const int no = nl * F * N;
+              vu = Real(0);
+              vp = Real(0);
+#pragma unroll
+              for (int j = 0; j < NP; ++j) {
+                const Real l = B.L[1 - s][j];
+                vu += l * xval(no + e * N + base + j * str);
+                vp += l * xval(no + DIM * N + base + j * str);
+              }
+            }
+            const Real tau_m = cst[7 + 2 * (2 * e + s)];
+            const Real tau_inv = cst[8 + 2 * (2 * e + s)];
+            const Real un_m = -nrm * vu;
+            lambda = (un_p + un_m + tau_p * tp[s] + tau_m * vp) * tau_inv;
+          } else {
+            const int id = -nb;
+            if (id == EW_BC_SOFT_WALL_ID) {
+              lambda = un_p * itau + tp[s];
+            } else if (id == EW_BC_ABSORBING_ID) {
+              lambda = Real(0.5) * tp[s] + Real(0.5) * un_p * itau;
+            } else {
+              if (id != EW_BC_HARD_WALL_ID) atomicOr(La.err, ERR_BAD_BOUNDARY_ID);
+              lambda = Real(0);
+            }
+          }
+          Fu[s] = (tp[s] - lambda) * rho_inv * nrm;
+          Fp[s] = rc2 * (-un_p + tau_p * (lambda - tp[s]));
+        }
+        // derivative of p and weighted transpose derivative of u_e
+        Real a1[4 + 1], b1[4], a2[4 + 1], b2[4];
+        eo_apply<NP, Real>(B.D, ep, op, pm, a1, b1);
+        eo_apply<NP, Real>(B.Dt, eu, ou, um, a2, b2);
+        const Real Fsu = Fu[0] + Fu[1], Fdu = Fu[0] - Fu[1];
+        const Real Fsp = Fp[0] + Fp[1], Fdp = Fp[0] - Fp[1];
+        const Real fu = bf * ih, fpp = bf * ih;
+        Real ku[NP], kp[NP];
+#pragma unroll
+        for (int i = 0; i < H; ++i) {
+          // u_e: -rho^{-1} (D p)_i + lift; p: rho c^2 (Dt u)_i + lift
+          const Real ua = -rho_inv * a1[i] + B.Wa[i] * Fdu;
+          const Real ub = -rho_inv * b1[i] + B.Ws[i] * Fsu;
+          ku[i] = fu * (ua + ub);
+          ku[NP - 1 - i] = fu * (ub - ua);
+          const Real pa = rc2 * a2[i] + B.Wa[i] * Fdp;
+          const Real pb = rc2 * b2[i] + B.Ws[i] * Fsp;
+          kp[i] = fpp * (pa + pb);
+          kp[NP - 1 - i] = fpp * (pb - pa);
+        }
+        if constexpr (NP % 2 == 1) {
+          ku[H] = fu * (-rho_inv * a1[H] + B.Wmid * Fsu);
+          kp[H] = fpp * (rc2 * a2[H] + B.Wmid * Fsp);
+        }
+        // pressure part of this direction to shared memory
+#pragma unroll
+        for (int i = 0; i < NP; ++i) sKp[(e * CB + cl) * N + base + i * str] = kp[i];
+        // finish u_e on this line (x-lines are contiguous: paired stores)
+        const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + e * N + base;
+        const int l0 = xo + e * N + base;
+        const int mode = sd.mode;
+        if (mode == MODE_APPLY) {
+#pragma unroll
+          for (int i = 0; i < NP; ++i) sd.Aout[g0 + i * str] = static_cast<double>(ku[i]);
+        } else {
+          const bool paired = NP % 2 == 0 && e == 0 &&
+                              (reinterpret_cast<uintptr_t>(sd.Aout) & 15) == 0 &&
+                              (reinterpret_cast<uintptr_t>(sd.Xout) & 7) == 0;
+#pragma unroll
+          for (int i = 0; i < NP; i += 2) {
+            OutT x0, x1 = OutT(0);
+            double a0, a1 = 0.0;
+            const double aa = stage_a ? sA[l0 + i * str] : sd.A[g0 + i * str];
+            update_point<Real, OutT>(sd, mode, aa, ku[i], x0, a0);
+            if (i + 1 < NP) {
+              const double ab = stage_a ? sA[l0 + (i + 1) * str] : sd.A[g0 + (i + 1) * str];
+              update_point<Real, OutT>(sd, mode, ab, ku[i + 1], x1, a1);
+            }
+            if (paired) {
+              if (mode == MODE_RK_MID) store2(static_cast<OutT*>(sd.Xout) + g0 + i, x0, x1);
+              store2(sd.Aout + g0 + i, a0, a1);
+            } else {
+              if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g0 + i * str] = x0;
+              sd.Aout[g0 + i * str] = a0;
+              if (i + 1 < NP) {
+                if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g0 + (i + 1) * str] = x1;
+                sd.Aout[g0 + (i + 1) * str] = a1;
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---------------------------------------------------------- pressure
+    const int src_local = sd.src_cell - wi.cell_begin;
+    Real src_val = Real(0);
+    if (src_local >= 0 && src_local < nc)
+      src_val = static_cast<Real>(sd.src_amp * ricker(*sd.time + sd.c_stage * sd.dt, sd.src_f0, sd.src_t0));
+    for (int idx = threadIdx.x; idx < nc * N; idx += blockDim.x) {
+      const int cl = idx / N;
+      const int q = idx - cl * N;
+      Real k = sKp[cl * N + q];
+#pragma unroll
+      for (int e = 1; e < DIM; ++e) k += sKp[(e * CB + cl) * N + q];
+      if (cl == src_local) k += src_val * static_cast<const Real*>(sd.src_w)[q];
+      const size_t g = ((size_t)wi.cell_begin + cl) * F * N + DIM * N + q;
+      const int lidx = cl * F * N + DIM * N + q;
+      const int mode = sd.mode;
+      if (mode == MODE_APPLY) {
+        sd.Aout[g] = static_cast<double>(k);
+      } else {
+        const double a = stage_a ? sA[lidx] : sd.A[g];
+        OutT xn;
+        double an;
+        update_point<Real, OutT>(sd, mode, a, k, xn, an);
+        if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g] = xn;
+        sd.Aout[g] = an;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace ew

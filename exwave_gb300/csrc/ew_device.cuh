@@ -56,7 +56,22 @@ struct SolveDesc {
   float bf;            // +1: M^-1 A(u); -1: second ADER step sign (boundary_fac)
   int32_t mode;
   int32_t pad;
+  const void* cellc;   // Real [cell][kCellConsts] constants of the Cartesian kernel
+  // point source in the pressure equation (batched solves): amplitude *
+  // Ricker(t) * phi_q(x_s) / JxW_q added to the pressure update of src_cell,
+  // at the stage time t = *time + c_stage * dt
+  const double* time;
+  const void* src_w;   // Real [points]
+  double src_amp, src_f0, src_t0, c_stage, dt;
+  int32_t src_cell;    // -1: none
+  int32_t pad2;
 };
+
+// Ricker wavelet (1 - 2 pi^2 f0^2 s^2) exp(-pi^2 f0^2 s^2), s = t - t0.
+__device__ __forceinline__ double ricker(double t, double f0, double t0) {
+  const double a = 9.869604401089358 * f0 * f0 * (t - t0) * (t - t0);
+  return (1.0 - 2.0 * a) * exp(-a);
+}
 
 struct WorkItem {
   int32_t solve;
@@ -142,13 +157,15 @@ __device__ __forceinline__ float f64_to_f32(double a) {
   return __uint_as_float(sign | ((unsigned int)e << 23) | m);
 }
 
+// Branch-free: a data-dependent early return lets the compiler if-convert
+// a following FP64 add into two adds and a select.
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned int u = __float_as_uint(f);
   const unsigned int sign = u & 0x80000000u;
   const unsigned int mag = u & 0x7fffffffu;
-  if (mag < 0x00800000u) return __longlong_as_double((long long)((unsigned long long)sign << 32));
-  const unsigned int hi = sign | ((mag >> 3) + (896u << 20));
-  const unsigned int lo = mag << 29;
+  const bool normal = mag >= 0x00800000u;
+  const unsigned int hi = sign | (normal ? ((mag >> 3) + (896u << 20)) : 0u);
+  const unsigned int lo = normal ? (mag << 29) : 0u;
   return __hiloint2double((int)hi, (int)lo);
 }
 

@@ -1,6 +1,7 @@
 // ew_inst.cu -- instantiates the kernels for one (dimension, points per
 // direction) pair, selected by -DEW_DIM and -DEW_NP, and exports their
 // launchers through a table (one object file per pair, compiled in parallel).
+#include "ew_cart.cuh"
 #include "ew_kernels.cuh"
 #include "ew_launch.h"
 
@@ -18,8 +19,17 @@ constexpr int DIM = EW_DIM;
 constexpr int NP = EW_NP;
 constexpr int N = ipow_c(NP, DIM);
 
+// Prefer the largest shared-memory carve-out: the kernels are limited by
+// resident CTAs, not by L1 hits.
+template <typename Kern>
+void carveout(Kern kern) {
+  cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       (int)cudaSharedmemCarveoutMaxShared);
+}
+
 template <typename Kern>
 cudaError_t run(Kern kern, const LaunchArgs& a, int grid, int block, size_t smem, cudaStream_t st) {
+  carveout(kern);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -30,6 +40,7 @@ cudaError_t run(Kern kern, const LaunchArgs& a, int grid, int block, size_t smem
 
 template <typename Kern>
 int blocks_per_sm(Kern kern, int block, size_t smem) {
+  carveout(kern);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int nb = 0;
@@ -61,6 +72,49 @@ struct CkK {
   }
 };
 
+template <typename Real, typename InT, typename OutT>
+struct CartK {
+  static size_t smem(int cb, int sx, int sa) {
+    return CartSmem<DIM, NP, Real, InT>(cb, sx != 0, sa != 0).end;
+  }
+  static cudaError_t launch(const LaunchArgs& a, int sx, int sa, int tma, int grid, cudaStream_t st) {
+    CartArgs ca;
+    ca.la = a;
+    ca.stage_x = sx;
+    ca.stage_a = sa;
+    ca.tma = tma;
+    const int cb = a.cells_per_block;
+    const size_t sm = smem(cb, sx, sa);
+    auto kern = stage_cart_kernel<DIM, NP, Real, InT, OutT>;
+    carveout(kern);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, cb * DIM * ipow_c(NP, DIM - 1), sm, st>>>(ca);
+    return cudaGetLastError();
+  }
+  static int occupancy(int cb, int sx, int sa) {
+    return blocks_per_sm(stage_cart_kernel<DIM, NP, Real, InT, OutT>, cb * DIM * ipow_c(NP, DIM - 1),
+                         smem(cb, sx, sa));
+  }
+};
+
+template <class K>
+void fill_cart(CartEntry& e) {
+  e.launch = &K::launch;
+  e.occupancy = &K::occupancy;
+  e.smem = &K::smem;
+}
+
+cudaError_t set_constants(const double* w, const double* D, const double* L0, const double* L1) {
+  const CartBasis<double> cd = make_cart_basis(NP, w, D, L0, L1);
+  const CartBasis<float> cf = cast_basis<float>(cd);
+  cudaError_t e = cudaMemcpyToSymbol(c_cart_d, &cd, sizeof(cd));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_cart_f, &cf, sizeof(cf));
+}
+
 template <class K>
 void fill(KernelEntry& e) {
   e.launch = &K::launch;
@@ -78,6 +132,11 @@ void EW_TABLE_FN(KernelTable& t) {
   t.dim = DIM;
   t.np = NP;
   t.points = N;
+  t.lines = DIM * ipow_c(NP, DIM - 1);
+  t.set_constants = &set_constants;
+  fill_cart<CartK<double, double, double>>(t.cart[STAGE_F64]);
+  fill_cart<CartK<float, double, float>>(t.cart[STAGE_MIX_IN64]);
+  fill_cart<CartK<float, float, float>>(t.cart[STAGE_MIX_IN32]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);

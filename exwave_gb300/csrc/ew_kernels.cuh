@@ -47,7 +47,7 @@ struct OpSmem {
     Fl = G + CB * DIM * S::N;
     geo = Fl + CB * 2 * DIM * S::FF * S::NF;
     mat = geo + CB * S::GEO;
-    end = (mat + CB * 2 + 3) & ~3;
+    end = (mat + CB * 4 + 3) & ~3;
   }
 };
 
@@ -92,8 +92,8 @@ __device__ __forceinline__ void load_block(const SolveDesc& sd, int cell_begin, 
   for (int i = threadIdx.x; i < total; i += blockDim.x) sX[i] = to_real<Real>(load_nc(X + i));
   const Real* G = static_cast<const Real*>(sd.geo) + (size_t)cell_begin * S::GEO;
   for (int i = threadIdx.x; i < nc * S::GEO; i += blockDim.x) sGeo[i] = load_nc(G + i);
-  const Real* M = static_cast<const Real*>(sd.mat) + (size_t)cell_begin * 2;
-  for (int i = threadIdx.x; i < nc * 2; i += blockDim.x) sMat[i] = load_nc(M + i);
+  const Real* M = static_cast<const Real*>(sd.mat) + (size_t)cell_begin * 4;
+  for (int i = threadIdx.x; i < nc * 4; i += blockDim.x) sMat[i] = load_nc(M + i);
 }
 
 // Cell term at point q of local cell cl: returns the velocity part
@@ -132,7 +132,7 @@ __device__ __forceinline__ void op_cell(const Real* sB, const Real* sX, Real* sG
   const Real det = cell_geom<DIM, Real, CART>(sGeo + cl * S::GEO, xi, JiT);
   const Real jxw = det * W;
   inv_jxw = Real(1) / jxw;
-  const Real rho = sMat[2 * cl], c = sMat[2 * cl + 1];
+  const Real rho = sMat[4 * cl], c = sMat[4 * cl + 1];
   const Real fu = -bf / rho;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
@@ -223,7 +223,7 @@ __device__ __forceinline__ void op_face(const Real* sB, const Real* sX, Real* sF
     for (int d = 0; d < DIM; ++d) nrm[d] *= il;
     jxw_f = wt * fabs(det) * len;
   }
-  const Real rho = sMat[2 * cl], c = sMat[2 * cl + 1];
+  const Real rho = sMat[4 * cl], c = sMat[4 * cl + 1];
   const Real rho_inv = Real(1) / rho, c_sq = c * c;
   const Real tau_p = Real(1) / (c * rho);
   Real un_p = Real(0);
@@ -253,8 +253,8 @@ __device__ __forceinline__ void op_face(const Real* sB, const Real* sX, Real* sF
         for (int j = 0; j < NP; ++j) a += Lm[j] * xm[fld * N + q0 + j * str];
         vm[fld] = a;
       }
-      rho_m = sMat[2 * nl];
-      c_m = sMat[2 * nl + 1];
+      rho_m = sMat[4 * nl];
+      c_m = sMat[4 * nl + 1];
     } else {
       const InT* xm = static_cast<const InT*>(sd.X) + (size_t)nb * F * N;
 #pragma unroll
@@ -267,8 +267,8 @@ __device__ __forceinline__ void op_face(const Real* sB, const Real* sX, Real* sF
         vm[fld] = a;
       }
       const Real* M = static_cast<const Real*>(sd.mat);
-      rho_m = load_nc(M + 2 * (size_t)nb);
-      c_m = load_nc(M + 2 * (size_t)nb + 1);
+      rho_m = load_nc(M + 4 * (size_t)nb);
+      c_m = load_nc(M + 4 * (size_t)nb + 1);
     }
     Real un_m = Real(0);
 #pragma unroll
@@ -599,8 +599,8 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
     const int cl = threadIdx.x / N;
     const int q = threadIdx.x - cl * N;
     const bool active = cl < nc;
-    const Real rho = active ? sMat[2 * cl] : Real(1);
-    const Real cc = active ? sMat[2 * cl + 1] : Real(1);
+    const Real rho = active ? sMat[4 * cl] : Real(1);
+    const Real cc = active ? sMat[4 * cl + 1] : Real(1);
     const Real c_sq = cc * cc;
     Real d1[F];
     if constexpr (POST) {

@@ -22,10 +22,23 @@ struct KernelEntry {
   size_t (*smem)(int cells_per_block) = nullptr;
 };
 
+// Launcher of the Cartesian line kernel (ew_cart.cuh).
+struct CartEntry {
+  cudaError_t (*launch)(const LaunchArgs&, int stage_x, int stage_a, int tma, int grid,
+                        cudaStream_t) = nullptr;
+  int (*occupancy)(int cells_per_block, int stage_x, int stage_a) = nullptr;
+  size_t (*smem)(int cells_per_block, int stage_x, int stage_a) = nullptr;
+};
+
 struct KernelTable {
   int dim = 0, np = 0, points = 0;
+  int lines = 0;  // threads per cell of the Cartesian kernel: dim * np^(dim-1)
   KernelEntry stage[N_STAGE_VARIANTS][2];  // [variant][cartesian]
+  CartEntry cart[N_STAGE_VARIANTS];
   KernelEntry ck[2][2][2];                 // [mixed][cartesian][post]
+  // upload the even-odd 1D constants of this degree to the current device
+  cudaError_t (*set_constants)(const double* w, const double* D, const double* L0,
+                               const double* L1) = nullptr;
 };
 
 #define EW_DECL(d, n) void kernel_table_d##d##_##n(KernelTable&);

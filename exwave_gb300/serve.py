@@ -1,0 +1,148 @@
+"""Serving loop with continuous batching.
+
+Requests (a solve: degree, mesh, material, source, receivers, end time)
+arrive over time; they wait in a FIFO queue until the device arena can hold
+them (admission by HBM budget), then join the resident batch.  Every tick
+advances all admitted solves by a few LSRK45 steps in one batched launch
+sequence, streams the new receiver samples to the host and retires the
+solves that reached their end time.  Solves that arrive while others run
+are admitted as soon as memory frees up, so their work overlaps on the
+device.  Latency = completion time - arrival time.
+"""
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from . import mesh as mesh_mod
+from .batch import Batch, Solve
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    degree: int
+    cells: int
+    speed: float
+    density: float
+    f0: float
+    source_pos: tuple
+    receivers: np.ndarray
+    end_time: float
+    dt: float = 0.0
+    n_steps: int = 0
+    admitted: float = None
+    finished: float = None
+    trace: list = field(default_factory=list)
+    samples_read: int = 0
+
+    def make_solve(self):
+        m = mesh_mod.hypercube(3, self.cells, speed=self.speed, density=self.density)
+        h = 1.0 / self.cells
+        self.dt = 0.25 * h / (self.speed * self.degree ** 1.5)
+        self.n_steps = max(1, int(np.ceil(self.end_time / self.dt - 1e-12)))
+        return Solve(m, self.degree, self.dt, self.n_steps,
+                     source=(list(self.source_pos), self.f0, 1.0 / self.f0, 1.0),
+                     receivers=self.receivers)
+
+    def dofs(self):
+        return self.cells ** 3 * 4 * (self.degree + 1) ** 3
+
+
+def draw_requests(n, rate, seed, degrees=(3, 7), cells=(8, 32), speed=(1.0, 4.0),
+                  density=(1.0, 3.0), f0=(2.0, 8.0), end_time=(0.2, 2.0), n_receivers=8):
+    """Seeded request stream: Poisson arrivals at `rate` per second and the
+    per-instance distribution of the batched configuration (degree uniform in
+    {3..7}, n^3 cells with n uniform in [8, 32], c ~ U[1,4], rho ~ U[1,3],
+    Ricker source f0 ~ U[2,8] at an interior point, 8 receivers)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n)) if rate > 0 else np.zeros(n)
+    reqs = []
+    for i in range(n):
+        reqs.append(Request(
+            rid=i, arrival=float(t[i]),
+            degree=int(rng.integers(degrees[0], degrees[1] + 1)),
+            cells=int(rng.integers(cells[0], cells[1] + 1)),
+            speed=float(rng.uniform(*speed)), density=float(rng.uniform(*density)),
+            f0=float(rng.uniform(*f0)),
+            source_pos=tuple(rng.uniform(0.2, 0.8, 3)),
+            receivers=rng.uniform(0.1, 0.9, (n_receivers, 3)),
+            end_time=float(rng.uniform(*end_time))))
+    return reqs
+
+
+class Server:
+    def __init__(self, precision="mixed", hbm_budget_bytes=150 << 30, steps_per_tick=4,
+                 max_solves=4096, device=0):
+        self.batch = Batch(precision=precision, hbm_budget_bytes=hbm_budget_bytes,
+                           max_solves=max_solves, device=device)
+        self.steps_per_tick = steps_per_tick
+
+    def run(self, requests, time_limit=None, log=None):
+        """Serve `requests` in real time; returns a statistics dict."""
+        b = self.batch
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        queue = deque()
+        active = {}
+        done = []
+        t0 = time.perf_counter()
+        dof_updates = 0
+        ticks = 0
+        peak_active = 0
+        while pending or queue or active:
+            now = time.perf_counter() - t0
+            if time_limit is not None and now >= time_limit:
+                break
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.popleft())
+            while queue:
+                r = queue[0]
+                solve = r.make_solve()
+                try:
+                    sid = b.add(solve)
+                except _lib.EwError as e:
+                    if e.code in (-4, -6):   # over the HBM budget / slot limit: wait
+                        break
+                    raise
+                r.admitted = time.perf_counter() - t0
+                active[sid] = r
+                queue.popleft()
+            peak_active = max(peak_active, len(active))
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, min(0.01, pending[0].arrival - now)))
+                continue
+            k = min(self.steps_per_tick, b.steps_left())
+            b.step(k)
+            b.synchronize()
+            ticks += 1
+            dof_updates += 5 * k * sum(r.dofs() for r in active.values())
+            for sid in list(active):
+                r = active[sid]
+                steps, total = b.info(sid)
+                if steps > r.samples_read:
+                    r.trace.append(b.receivers(sid, r.samples_read, steps - r.samples_read))
+                    r.samples_read = steps
+                if steps >= total:
+                    r.finished = time.perf_counter() - t0
+                    b.remove(sid)
+                    del active[sid]
+                    done.append(r)
+                    if log:
+                        log(r)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.finished - r.arrival for r in done]) if done else np.array([])
+        wait = np.array([r.admitted - r.arrival for r in done]) if done else np.array([])
+        return {
+            "completed": len(done), "offered": len(requests), "wall_s": wall,
+            "solves_per_s": len(done) / wall if wall > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "admission_wait_p50_s": float(np.percentile(wait, 50)) if len(wait) else None,
+            "backlog_at_end": len(queue) + len(pending), "active_at_end": len(active),
+            "peak_active": peak_active, "ticks": ticks,
+            "dof_updates_per_s": dof_updates / wall if wall > 0 else 0.0,
+        }

@@ -172,6 +172,67 @@ int64_t ew_hypercube_n_cells(const ew_hypercube_desc* desc);
  * neighbors[n_cells][2*dim] in the ew_mesh_desc conventions. */
 int ew_hypercube_mesh(const ew_hypercube_desc* desc, double* vertices, int32_t* neighbors);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent solves (uneven degree, mesh size, material, source) in
+ * one device-resident batch: each step advances every unfinished solve by
+ * one LSRK45 step with one persistent launch per (dimension, degree) group
+ * and stage over a work list of cell blocks; the per-step launch sequence is
+ * captured as a CUDA graph.  Admission is bounded by an HBM budget (device
+ * arena allocated once).  No reference counterpart: the reference advances
+ * one mesh per MPI job. */
+typedef struct ew_batch ew_batch;
+
+typedef struct ew_batch_options {
+  int32_t precision;        /* ew_precision */
+  int32_t device;
+  int64_t hbm_budget_bytes; /* arena size */
+  int32_t max_solves;
+  int32_t use_graphs;       /* 1: capture each step as a CUDA graph */
+} ew_batch_options;
+
+/* Ricker point source added to the pressure equation:
+ * amplitude * (1 - 2 pi^2 f0^2 s^2) exp(-pi^2 f0^2 s^2), s = t - delay. */
+typedef struct ew_source_desc {
+  double position[3];
+  double frequency;
+  double delay;
+  double amplitude;
+} ew_source_desc;
+
+typedef struct ew_solve_desc {
+  ew_mesh_desc mesh;        /* Cartesian cells */
+  double dt;
+  int64_t n_steps;          /* the solve ends after n_steps LSRK45 steps */
+  int32_t n_sources;        /* 0 or 1 */
+  ew_source_desc source;
+  int32_t n_receivers;      /* pressure sampled after every step */
+  const double* receivers;  /* host [n_receivers][dim] */
+} ew_solve_desc;
+
+int ew_batch_create(const ew_batch_options* options, ew_batch** batch);
+void ew_batch_destroy(ew_batch* batch);
+const char* ew_batch_last_error(const ew_batch* batch);
+/* Device bytes a solve would take from the arena. */
+int64_t ew_batch_solve_bytes(const ew_batch* batch, const ew_solve_desc* solve);
+int64_t ew_batch_bytes_free(const ew_batch* batch);
+/* Admits a solve (zero initial state); EW_ERR_OOM when the arena cannot hold it. */
+int ew_batch_add(ew_batch* batch, const ew_solve_desc* solve, int32_t* id);
+/* Releases a solve's memory. */
+int ew_batch_remove(ew_batch* batch, int32_t id);
+/* Copies a caller's device FP64 state (canonical layout) into a solve. */
+int ew_batch_set_state(ew_batch* batch, int32_t id, const double* state);
+/* Copies a solve's current FP64 state to a caller's device buffer. */
+int ew_batch_get_state(ew_batch* batch, int32_t id, double* state);
+/* Advances every unfinished solve by n_steps (at most the smallest number
+ * of steps any unfinished solve has left). */
+int ew_batch_step(ew_batch* batch, int32_t n_steps);
+int ew_batch_info(const ew_batch* batch, int32_t id, int64_t* steps_done, int64_t* n_steps);
+/* Receiver samples [first, first + count) of a solve into host out[count][n_receivers]. */
+int ew_batch_receivers(ew_batch* batch, int32_t id, int64_t first, int64_t count, double* out);
+int ew_batch_set_stream(ew_batch* batch, void* stream);
+int ew_batch_synchronize(ew_batch* batch);
+int64_t ew_batch_kernel_launches(const ew_batch* batch);
+
 /* Waits for the context's stream and reports a raised device error flag. */
 int ew_synchronize(ew_ctx* ctx);
 

@@ -1062,6 +1062,126 @@ int ewo_run_reference(ewo_problem* p, int integrator, double cfl, double final_t
   return nrows;
 }
 
+// ---- extensions without a reference counterpart (point sources, receivers)
+
+// Cell containing x and its reference coordinates (Newton on the
+// multilinear map, after a bounding-box test).
+static bool ewo_locate(const Oracle* O, const double* x, int64_t* cell, double* xi) {
+  const int dim = O->dim, nv = 1 << dim;
+  for (int64_t c = 0; c < O->mesh.n_cells; ++c) {
+    const double* V = &O->mesh.vert[(size_t)c * nv * dim];
+    bool in = true;
+    for (int e = 0; e < dim && in; ++e) {
+      double lo = 1e300, hi = -1e300;
+      for (int v = 0; v < nv; ++v) {
+        lo = std::min(lo, V[v * dim + e]);
+        hi = std::max(hi, V[v * dim + e]);
+      }
+      if (x[e] < lo - 1e-12 || x[e] > hi + 1e-12) in = false;
+    }
+    if (!in) continue;
+    double r[3] = {0.5, 0.5, 0.5};
+    for (int it = 0; it < 50; ++it) {
+      double y[3] = {0, 0, 0}, J[3][3], JiT[3][3];
+      map_point(dim, V, r, y);
+      jacobian(dim, V, r, J);
+      inverse_transpose(dim, J, JiT);
+      double step = 0.0;
+      for (int e = 0; e < dim; ++e) {
+        double d = 0.0;  // (J^{-1} (x - y))_e = sum_d JiT[d][e] (x-y)_d
+        for (int dd = 0; dd < dim; ++dd) d += JiT[dd][e] * (x[dd] - y[dd]);
+        r[e] += d;
+        step += std::fabs(d);
+      }
+      if (step < 1e-15) break;
+    }
+    bool inside = true;
+    for (int e = 0; e < dim; ++e)
+      if (r[e] < -1e-10 || r[e] > 1 + 1e-10) inside = false;
+    if (!inside) continue;
+    *cell = c;
+    for (int e = 0; e < dim; ++e) xi[e] = r[e];
+    return true;
+  }
+  return false;
+}
+
+// Pressure of the DG field u at physical points (receivers): out[i].
+int ewo_point_values(ewo_problem* p, const double* u, int n, const double* pts, double* out) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  for (int i = 0; i < n; ++i) {
+    int64_t c;
+    double xi[3] = {0, 0, 0};
+    if (!ewo_locate(O, pts + i * O->dim, &c, xi)) {
+      g_last_error = "point outside the mesh";
+      return -1;
+    }
+    double v = 0.0;
+    for (int q = 0; q < O->N; ++q) {
+      int ii[3] = {0, 0, 0};
+      O->point_index(q, ii);
+      double w = 1.0;
+      for (int e = 0; e < O->dim; ++e) w *= O->B.lag.value(ii[e], xi[e]);
+      v += w * u[(size_t)c * O->F * O->N + O->dim * O->N + q];
+    }
+    out[i] = v;
+  }
+  return 0;
+}
+
+// LSRK45 step with a Ricker point source amp*(1-2a)exp(-a), a = pi^2 f0^2
+// (t-delay)^2, added to the pressure equation at the stage times
+// t + c_s dt: the term amp*r(t) phi_q(x_s) / JxW_q on the source cell.
+int ewo_lsrk45_step_source(ewo_problem* p, double dt, double t, double* vec_n, double* vec_np,
+                           const double* xs, double amp, double f0, double delay) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  int64_t cell;
+  double xi[3] = {0, 0, 0};
+  if (!ewo_locate(O, xs, &cell, xi)) {
+    g_last_error = "source outside the mesh";
+    return -1;
+  }
+  std::vector<double> w(O->N);
+  for (int q = 0; q < O->N; ++q) {
+    int ii[3] = {0, 0, 0};
+    O->point_index(q, ii);
+    double phi = 1.0, r[3] = {0, 0, 0};
+    for (int e = 0; e < O->dim; ++e) {
+      phi *= O->B.lag.value(ii[e], xi[e]);
+      r[e] = O->B.rule.x[ii[e]];
+    }
+    double JiT[3][3];
+    const double det = O->geom(cell, r, JiT);
+    w[q] = phi / (det * O->W[q]);
+  }
+  const double a21 = 970286171893. / 4311952581923.;
+  const double a32 = 6584761158862. / 12103376702013.;
+  const double a43 = 2251764453980. / 15575788980749.;
+  const double a54 = 26877169314380. / 34165994151039.;
+  const double b1 = 1153189308089. / 22510343858157.;
+  const double b2 = 1772645290293. / 4653164025191.;
+  const double b3 = -1672844663538. / 4480602732383.;
+  const double b4 = 2114624349019. / 3568978502595.;
+  const double b5 = 5198255086312. / 14908931495163.;
+  const double A[5] = {a21, a32, a43, a54, b5};
+  const double Bm[5] = {b1 - a21, b2 - a32, b3 - a43, b4 - a54, 0.0};
+  const double cs[5] = {0.0, a21, b1 + a32, b1 + b2 + a43, b1 + b2 + b3 + a54};
+  const int64_t nd = (int64_t)O->n_dofs();
+  std::vector<double> tmp(nd);
+  double* in[5] = {vec_n, vec_n, vec_np, vec_n, vec_np};
+  double* v2[5] = {vec_n, vec_np, vec_n, vec_np, vec_np};
+  double* v3[5] = {vec_np, vec_n, vec_np, vec_n, vec_n};
+  for (int st = 0; st < 5; ++st) {
+    O->apply(in[st], tmp.data());
+    const double ts = t + cs[st] * dt;
+    const double aa = kPi * kPi * f0 * f0 * (ts - delay) * (ts - delay);
+    const double r = amp * (1.0 - 2.0 * aa) * std::exp(-aa);
+    for (int q = 0; q < O->N; ++q) tmp[(size_t)cell * O->F * O->N + O->dim * O->N + q] += r * w[q];
+    ewo_rk_update(nd, A[st] * dt, Bm[st] * dt, st == 4, tmp.data(), v2[st], v3[st]);
+  }
+  return 0;
+}
+
 int ewo_num_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();

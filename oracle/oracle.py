@@ -70,6 +70,11 @@ def lib():
         L.ewo_run_reference.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, dp,
                                         ctypes.c_int, dp]
+        L.ewo_point_values.restype = ctypes.c_int
+        L.ewo_point_values.argtypes = [P, dp, ctypes.c_int, dp, dp]
+        L.ewo_lsrk45_step_source.restype = ctypes.c_int
+        L.ewo_lsrk45_step_source.argtypes = [P, ctypes.c_double, ctypes.c_double, dp, dp, dp,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.ewo_last_error.restype = ctypes.c_char_p
         L.ewo_num_threads.restype = ctypes.c_int
         _lib = L
@@ -193,6 +198,21 @@ class Problem:
         lib().ewo_errors_modes(self.h, _dp(np.ascontiguousarray(u)), len(amps), _dp(amps),
                                kv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), t, _dp(out))
         return out
+
+    def point_values(self, u, points):
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        out = np.zeros(pts.shape[0])
+        if lib().ewo_point_values(self.h, _dp(np.ascontiguousarray(u)), pts.shape[0], _dp(pts),
+                                  _dp(out)) != 0:
+            raise RuntimeError(lib().ewo_last_error().decode())
+        return out
+
+    def lsrk45_step_source(self, dt, t, vec_n, vec_np, xs, amp, f0, delay):
+        x = np.zeros(3)
+        x[:len(xs)] = xs
+        if lib().ewo_lsrk45_step_source(self.h, dt, t, _dp(vec_n), _dp(vec_np), _dp(x), amp, f0,
+                                        delay) != 0:
+            raise RuntimeError(lib().ewo_last_error().decode())
 
     def run_reference(self, integrator, cfl, final_time, tick, modes, max_time_steps=1000000):
         rows = np.zeros((4096, 5))
