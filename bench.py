@@ -346,7 +346,7 @@ def batch_workload(args, torch):
     for s in solves:
         b.add(s)
     dofs = sum(r.dofs() for r in reqs)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: the batch replays its graphs on it
     b.set_stream(stream)
     b.step(args.warmup)
     b.synchronize()

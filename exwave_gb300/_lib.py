@@ -25,7 +25,8 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_batch_create", "ew_batch_destroy", "ew_batch_last_error", "ew_batch_solve_bytes",
            "ew_batch_bytes_free", "ew_batch_add", "ew_batch_remove", "ew_batch_set_state",
            "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_receivers",
-           "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches"]
+           "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches",
+           "ew_tune_set", "ew_tune_get"]
 
 
 class EwError(RuntimeError):
@@ -90,13 +91,32 @@ def load():
         "ew_hypercube_mesh": (ctypes.c_int, [ctypes.POINTER(HypercubeDesc), dp, i32p]),
         "ew_synchronize": (ctypes.c_int, [vp]),
         "ew_kernel_launches": (i64, [vp]),
+        "ew_tune_set": (ctypes.c_int, [i32, i32, i32, i32]),
+        "ew_tune_get": (i32, [i32, i32, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
     _lib = L
+    _apply_tuning(L)
     return L
+
+
+def _apply_tuning(L):
+    """Load the tuned cells-per-block table of this GPU model, if any."""
+    import json
+    path = os.path.join(HERE, "tuning", "tuning.json")
+    if not os.path.exists(path):
+        return
+    try:
+        with open(path) as f:
+            table = json.load(f)
+    except (OSError, ValueError):
+        return
+    for e in table.get("entries", []):
+        L.ew_tune_set(int(e["dim"]), int(e["degree"]), 1 if e["precision"] == "mixed" else 0,
+                      int(e["cells_per_block"]))
 
 
 def check(rc, ctx=None):

@@ -1,0 +1,106 @@
+"""Autotuner of the operator kernel's cells per thread block.
+
+For every (dimension, degree, precision) it builds a Cartesian membrane
+problem of about `target_dofs` DoFs, times LSRK45 steps with each admissible
+cells-per-block value (threads per block = cells x lines of the Cartesian
+kernel, at most 256) and keeps the fastest.  The table is written to
+exwave_gb300/tuning/tuning.json and loaded by the library at import
+(``ew_tune_set``), where ew_create and the batch runtime use it.
+
+Usage on the GPU: python -m exwave_gb300.autotune [--target-dofs 4e7]
+"""
+import argparse
+import json
+import os
+
+import numpy as np
+
+from . import _lib
+from . import mesh as mesh_mod
+from .operator import WaveEquationOperation
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TABLE = os.path.join(HERE, "tuning", "tuning.json")
+
+
+def lines_per_cell(dim, degree):
+    return dim * (degree + 1) ** (dim - 1)
+
+
+def candidates(dim, degree):
+    lim = max(1, 256 // lines_per_cell(dim, degree))
+    c = sorted({1, 2, 3, 4, 6, 8, 12, 16, 24, 32, lim} & set(range(1, lim + 1)))
+    return c
+
+
+def time_case(dim, degree, precision, cells, cb, steps, torch):
+    m = mesh_mod.hypercube(dim, cells)
+    dt = mesh_mod.time_step_size(m, 0.25 / degree ** 1.5)
+    op = WaveEquationOperation(m, degree, precision=precision, cells_per_block=cb)
+    u = op.project_membrane([1.0], [[1] * dim])
+    v = torch.zeros_like(u)
+    op.lsrk45_step(dt, u, v)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+    op.set_stream(stream)
+    e0.record(stream)
+    for _ in range(steps):
+        op.lsrk45_step(dt, u, v)
+        u, v = v, u
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    n = op.n_dofs
+    op.close()
+    return n * 5 * steps / (ms / 1e3)
+
+
+def run(dims=(2, 3), degrees=range(1, 8), precisions=("mixed", "fp64"), target_dofs=4e7, steps=4,
+        log=print):
+    import torch
+    entries = []
+    for dim in dims:
+        for k in degrees:
+            dofs_per_cell = (dim + 1) * (k + 1) ** dim
+            cells = max(4, int(round((target_dofs / dofs_per_cell) ** (1.0 / dim))))
+            for prec in precisions:
+                best = None
+                res = {}
+                for cb in candidates(dim, k):
+                    rate = time_case(dim, k, prec, cells, cb, steps if prec == "mixed" else 2, torch)
+                    res[cb] = rate
+                    if best is None or rate > res[best]:
+                        best = cb
+                entries.append({"dim": dim, "degree": k, "precision": prec,
+                                "cells_per_block": best, "cells": cells,
+                                "rates": {str(c): r for c, r in res.items()}})
+                if log:
+                    log("dim %d k %d %s: best cb %d (%.3g DoF-updates/s)" % (dim, k, prec, best,
+                                                                          res[best]))
+    return entries
+
+
+def save(entries, gpu_name):
+    os.makedirs(os.path.dirname(TABLE), exist_ok=True)
+    with open(TABLE, "w") as f:
+        json.dump({"gpu": gpu_name, "entries": entries}, f, indent=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--target-dofs", type=float, default=4e7)
+    ap.add_argument("--dims", default="2,3")
+    ap.add_argument("--precisions", default="mixed,fp64")
+    args = ap.parse_args()
+    import torch
+    _lib.load()
+    entries = run(dims=[int(d) for d in args.dims.split(",")],
+                  precisions=args.precisions.split(","), target_dofs=args.target_dofs)
+    save(entries, torch.cuda.get_device_name(0))
+    print("wrote", TABLE)
+
+
+if __name__ == "__main__":
+    main()

@@ -47,6 +47,18 @@ const KernelTable& kernel_table(int dim, int np) {
   return g_tables[dim - 2][np];
 }
 
+namespace {
+int g_tuned[2][EW_MAX_DEGREE + 1][2] = {};
+std::mutex g_tuned_mutex;
+}  // namespace
+
+int tuned_cells_per_block(int dim, int degree, int precision) {
+  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 || precision > 1)
+    return 0;
+  std::lock_guard<std::mutex> lk(g_tuned_mutex);
+  return g_tuned[dim - 2][degree][precision];
+}
+
 cudaError_t upload_cart_constants(int dim, int np) {
   GaussRule g = gauss_rule(np);
   std::vector<double> D(np * np), L0(np), L1(np);
@@ -491,8 +503,19 @@ void split(double v, float* hi, float* lo) {
   *lo = (float)(v - (double)*hi);
 }
 
-int launch_stage(ew_ctx* c, int variant, const double* A, const void* X, void* Xout, double* Aout,
-                 int mode, double f1, double f2, float bf) {
+bool cart_variant_in32(int cv) {
+  return cv == ew::CV_MIX_APPLY32 || cv == ew::CV_MIX_MID || cv == ew::CV_MIX_LAST ||
+         cv == ew::CV_MIX_UPD;
+}
+bool cart_variant_apply(int cv) {
+  return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32;
+}
+
+// One operator launch.  `variant` selects the general (curved-cell) kernel,
+// `cvar` the Cartesian line kernel; the context uses the one that fits its
+// mesh.
+int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* X, void* Xout,
+                 double* Aout, int mode, double f1, double f2, float bf) {
   ew::LaunchArgs a = base_args(c, false);
   a.single.X = X;
   a.single.A = A;
@@ -508,21 +531,21 @@ int launch_stage(ew_ctx* c, int variant, const double* A, const void* X, void* X
   cudaError_t e;
   if (c->cart) {
     // line kernel: stage X unless it is the accumulator itself (first LSRK
-    // stage), stage A in the RK modes; bulk copies need 16-byte alignment
-    const size_t in_sz = variant == ew::STAGE_MIX_IN32 ? 4 : 8;
-    const int sa = mode != ew::MODE_APPLY ? 1 : 0;
+    // stage); bulk copies need 16-byte alignment
+    const size_t in_sz = cart_variant_in32(cvar) ? 4 : 8;
+    const bool sa = !cart_variant_apply(cvar);
     const int sx = (sa && static_cast<const void*>(A) == X && in_sz == 8) ? 0 : 1;
     const size_t cell_elems = (size_t)c->F * c->N;
     const bool tma = (cell_elems * in_sz) % 16 == 0 && (cell_elems * 8) % 16 == 0 &&
                      (reinterpret_cast<uintptr_t>(X) % 16) == 0 &&
-                     (reinterpret_cast<uintptr_t>(A) % 16) == 0;
+                     (!sa || (reinterpret_cast<uintptr_t>(A) % 16) == 0);
     a.work = c->d_work_cart;
     a.n_work = c->n_work_cart;
     a.cells_per_block = c->cb_cart;
-    const ew::CartEntry& k = c->kt->cart[variant];
-    const int occ = std::max(1, k.occupancy(c->cb_cart, sx, sa));
+    const ew::CartEntry& k = c->kt->cart[cvar];
+    const int occ = std::max(1, k.occupancy(c->cb_cart, sx));
     const int grid = std::max(1, std::min(c->n_work_cart, occ * c->num_sms));
-    e = k.launch(a, sx, sa, tma ? 1 : 0, grid, c->stream);
+    e = k.launch(a, sx, tma ? 1 : 0, grid, c->stream);
   } else {
     const ew::KernelEntry& k = c->kt->stage[variant][0];
     e = k.launch(a, c->grid_stage[variant], c->stream);
@@ -710,10 +733,12 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     --c->cb_ck;
   if (cart) {
     const int lines = c->kt->lines;
-    c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block : std::max(1, 256 / lines);
+    const int tuned = ew::tuned_cells_per_block(c->dim, c->degree, opt.precision);
+    c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block
+                                         : (tuned > 0 ? tuned : std::max(1, 256 / lines));
     c->cb_cart = std::max(1, std::min(c->cb_cart, 256 / lines));
-    const int v = c->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
-    while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1, 1) > 110 * 1024) --c->cb_cart;
+    const int v = c->mixed ? ew::CV_MIX_MID : ew::CV_F64_MID;
+    while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1) > 110 * 1024) --c->cb_cart;
   }
   if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
       (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)) ||
@@ -759,7 +784,8 @@ int ew_apply(ew_ctx* ctx, const double* src, double* dst) {
   if (rc) return rc;
   if (!src || !dst || src == dst) return fail(ctx, EW_ERR_INVALID, "ew_apply: src/dst invalid");
   const int var = ctx->mixed ? ew::STAGE_MIX_IN64 : ew::STAGE_F64;
-  return launch_stage(ctx, var, nullptr, src, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, 1.0f);
+  const int cv = ctx->mixed ? ew::CV_MIX_APPLY64 : ew::CV_F64_APPLY;
+  return launch_stage(ctx, var, cv, nullptr, src, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, 1.0f);
 }
 
 int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const double* v1, double* v2,
@@ -798,22 +824,24 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
       double* Ao;
     } st[5] = {{N, N, T, P}, {T, P, P, N}, {P, N, N, T}, {N, T, T, P}, {T, P, nullptr, P}};
     for (int s = 0; s < 5; ++s) {
-      rc = launch_stage(ctx, STAGE_F64, st[s].A, st[s].X, st[s].Xo, st[s].Ao,
-                        s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+      rc = launch_stage(ctx, STAGE_F64, s < 4 ? CV_F64_MID : CV_F64_LAST, st[s].A, st[s].X,
+                        st[s].Xo, st[s].Ao, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
       if (rc) return rc;
     }
     return EW_OK;
   }
-  // mixed: FP64 accumulator in vec_np (in place), FP32 stage inputs ping-pong
+  // mixed: accumulator in vec_np (in place; on Cartesian meshes a float-float
+  // pair between the stages, FP64 at the end), FP32 stage inputs ping-pong
   float* X0 = ctx->d_x32[0];
   float* X1 = ctx->d_x32[1];
-  rc = launch_stage(ctx, STAGE_MIX_IN64, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0], f2[0], 1.0f);
+  rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0],
+                    f2[0], 1.0f);
   if (rc) return rc;
   const float* xin[4] = {X0, X1, X0, X1};
   float* xout[4] = {X1, X0, X1, nullptr};
   for (int s = 1; s < 5; ++s) {
-    rc = launch_stage(ctx, STAGE_MIX_IN32, vec_np, xin[s - 1], xout[s - 1], vec_np,
-                      s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+    rc = launch_stage(ctx, STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1],
+                      xout[s - 1], vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
     if (rc) return rc;
   }
   return EW_OK;
@@ -826,7 +854,8 @@ int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst) {
   void* T = ctx->mixed ? static_cast<void*>(ctx->d_x32[0]) : static_cast<void*>(ctx->d_tmp64);
   if ((rc = launch_ck(ctx, dt, src, T))) return rc;
   const int var = ctx->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
-  return launch_stage(ctx, var, nullptr, T, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, -1.0f);
+  const int cv = ctx->mixed ? ew::CV_MIX_APPLY32 : ew::CV_F64_APPLY;
+  return launch_stage(ctx, var, cv, nullptr, T, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, -1.0f);
 }
 
 int ew_ader_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np) {
@@ -837,8 +866,9 @@ int ew_ader_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np) {
   void* T = ctx->mixed ? static_cast<void*>(ctx->d_x32[0]) : static_cast<void*>(ctx->d_tmp64);
   if ((rc = launch_ck(ctx, dt, vec_n, T))) return rc;
   const int var = ctx->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
+  const int cv = ctx->mixed ? ew::CV_MIX_UPD : ew::CV_F64_LAST;
   // vec_np = vec_n - (-M^{-1}A(T)) = vec_n + M^{-1}A(T)
-  return launch_stage(ctx, var, vec_n, T, nullptr, vec_np, ew::MODE_RK_LAST, 1.0, 0.0, 1.0f);
+  return launch_stage(ctx, var, cv, vec_n, T, nullptr, vec_np, ew::MODE_RK_LAST, 1.0, 0.0, 1.0f);
 }
 
 int ew_quadrature_points(ew_ctx* ctx, double* xyz) {
@@ -942,6 +972,19 @@ int ew_l2_difference(ew_ctx* ctx, const double* a, const double* b, double out[2
   out[0] = o3[0];
   out[1] = o3[1];
   return rc;
+}
+
+int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_per_block) {
+  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 ||
+      precision > 1 || cells_per_block < 0 || cells_per_block > 1024)
+    return EW_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ew::g_tuned_mutex);
+  ew::g_tuned[dim - 2][degree][precision] = cells_per_block;
+  return EW_OK;
+}
+
+int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision) {
+  return ew::tuned_cells_per_block(dim, degree, precision);
 }
 
 int ew_synchronize(ew_ctx* ctx) {

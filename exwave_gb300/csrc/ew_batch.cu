@@ -147,7 +147,7 @@ struct Group {
   ew::WorkItem* d_work = nullptr;
   int n_work = 0;
   int grid[2][5] = {{0}};
-  int sx[5] = {0}, sa[5] = {0}, variant[5] = {0};
+  int sx[5] = {0}, variant[5] = {0};
   int tma = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
@@ -362,17 +362,20 @@ int rebuild(ew_batch* b) {
     g.members = kv.second;
     const ew::KernelTable& kt = ew::kernel_table(g.dim, g.np);
     const int lines = kt.lines;
-    g.cb = std::max(1, 256 / lines);
+    const int tuned = ew::tuned_cells_per_block(g.dim, g.np - 1, b->mixed ? 1 : 0);
+    g.cb = tuned > 0 ? std::min(tuned, std::max(1, 256 / lines)) : std::max(1, 256 / lines);
     const int NP = g.np;
     int N = 1;
     for (int d = 0; d < g.dim; ++d) N *= NP;
     const int F = g.dim + 1;
     for (int st = 0; st < 5; ++st) {
-      g.variant[st] = b->mixed ? (st == 0 ? ew::STAGE_MIX_IN64 : ew::STAGE_MIX_IN32) : ew::STAGE_F64;
-      g.sa[st] = 1;
+      if (b->mixed)
+        g.variant[st] = st == 0 ? ew::CV_MIX_S1 : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST);
+      else
+        g.variant[st] = st < 4 ? ew::CV_F64_MID : ew::CV_F64_LAST;
       g.sx[st] = (st == 0) ? 0 : 1;  // first stage: X is the accumulator
     }
-    while (g.cb > 1 && kt.cart[g.variant[1]].smem(g.cb, 1, 1) > 110 * 1024) --g.cb;
+    while (g.cb > 1 && kt.cart[g.variant[1]].smem(g.cb, 1) > 110 * 1024) --g.cb;
     const size_t cell_x = (size_t)F * N * (b->mixed ? 4 : 8);
     g.tma = (cell_x % 16 == 0) && (((size_t)F * N * 8) % 16 == 0);
     // tables
@@ -406,7 +409,7 @@ int rebuild(ew_batch* b) {
     }
     for (int p = 0; p < 2; ++p)
       for (int st = 0; st < 5; ++st) {
-        const int occ = std::max(1, kt.cart[g.variant[st]].occupancy(g.cb, g.sx[st], g.sa[st]));
+        const int occ = std::max(1, kt.cart[g.variant[st]].occupancy(g.cb, g.sx[st]));
         g.grid[p][st] = std::max(1, std::min(g.n_work, occ * b->num_sms));
       }
     if ((e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -467,7 +470,7 @@ int launch_step(ew_batch* b, int p) {
       a.n_work = g.n_work;
       a.cells_per_block = g.cb;
       a.err = b->d_err;
-      e = kt.cart[g.variant[st]].launch(a, g.sx[st], g.sa[st], g.tma, g.grid[p][st], g.stream);
+      e = kt.cart[g.variant[st]].launch(a, g.sx[st], g.tma, g.grid[p][st], g.stream);
       if (e != cudaSuccess) return bcuda(b, e, "batch stage launch");
       ++n;
     }

@@ -20,6 +20,7 @@
 #pragma once
 
 #include <cstring>
+#include <type_traits>
 
 #include "ew_kernels.cuh"
 
@@ -175,6 +176,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// Ampere-style asynchronous copies (LDGSTS) of 4 or 8 bytes into shared memory.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src),
+               "n"(BYTES)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Bounded wait for the phase with the given parity; false on time-out.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_addr(bar);
@@ -200,7 +211,7 @@ template <int DIM, int NP, typename Real, typename InT>
 struct CartSmem {
   static constexpr int N = ipow_c(NP, DIM);
   static constexpr int F = DIM + 1;
-  size_t bar, X, A, Kp, cell, end;
+  size_t bar, X, A, Kp, cell, nb, end;
   int xbytes, abytes;  // per buffer
   __host__ __device__ CartSmem(int CB, bool stage_x, bool stage_a) {
     bar = 0;  // 4 mbarriers (X and A, double buffered)
@@ -210,35 +221,100 @@ struct CartSmem {
     abytes = stage_a ? CB * F * N * (int)sizeof(double) : 0;
     Kp = A + 2 * (size_t)((abytes + 127) & ~127);
     cell = Kp + (size_t)DIM * CB * N * sizeof(Real);
-    end = cell + (size_t)CB * kCellConsts * sizeof(Real);
+    // per thread: the neighbours' lines of u_e and p on both sides
+    nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
+    const int threads = CB * DIM * ipow_c(NP, DIM - 1);
+    end = nb + (size_t)threads * 4 * NP * sizeof(InT);
     end = (end + 127) & ~(size_t)127;
   }
 };
 
-// Stage update of one value: RK_MID gives the next stage input (xn) and
-// accumulator (an), RK_LAST the accumulator.  FP64 path: the reference's
-// RKVectorUpdater arithmetic; mixed path: FP32 increment added to the FP64
-// accumulator, conversions on the integer pipe.
-template <typename Real, typename OutT>
-__device__ __forceinline__ void update_point(const SolveDesc& sd, int mode, double a, Real k,
-                                             OutT& xn, double& an) {
-  if constexpr (sizeof(Real) == 8) {
-    if (mode == MODE_RK_MID) {
-      const double x = a + sd.f1 * k;
-      xn = static_cast<OutT>(x);
-      an = x + sd.f2 * k;
-    } else {
-      xn = OutT(0);
-      an = a + sd.f1 * k;
-    }
-  } else {
-    if (mode == MODE_RK_MID) {
-      xn = static_cast<OutT>(fmaf(sd.f1f, k, f64_to_f32(a)));
-      an = a + f32_to_f64(fmaf(sd.fb_hi, k, sd.fb_lo * k));
-    } else {
-      xn = OutT(0);
-      an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
-    }
+// Epilogues of the stage kernel (compile-time, so that no FP64 work of
+// an unused branch is if-converted into the executed path).
+//  APPLY       : Aout = k (WaveEquationOperation::apply)
+//  F64_MID/LAST: the reference's RKVectorUpdater arithmetic in FP64
+//  MIX_S1      : first LSRK stage, FP64 state in, FP32 stage input and
+//                float-float accumulator out
+//  MIX_MID     : float-float accumulator in and out, FP32 stage input out
+//  MIX_LAST    : float-float accumulator in, FP64 state out
+//  MIX_UPD     : FP64 in, FP64 out (ADER update u + k)
+// Within an LSRK step the mixed path keeps the accumulator as an unevaluated
+// sum hi + lo of two floats (about 48 significant bits) in the 8-byte slot
+// of the FP64 vector, updated with error-free transformations on the FP32
+// pipes; the FP64 pipe is used only where the step begins and ends.
+enum Epi : int {
+  EPI_APPLY = 0,
+  EPI_F64_MID = 1,
+  EPI_F64_LAST = 2,
+  EPI_MIX_S1 = 3,
+  EPI_MIX_MID = 4,
+  EPI_MIX_LAST = 5,
+  EPI_MIX_UPD = 6
+};
+
+template <int EPI>
+struct EpiTraits {
+  static constexpr bool stage_a = EPI != EPI_APPLY;
+  static constexpr bool writes_x = EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID;
+};
+
+// (hi, lo) + b with hi + lo normalised (Knuth two-sum, fast renormalisation)
+__device__ __forceinline__ void ff_add(float hi, float lo, float b, float& rh, float& rl) {
+  const float s = __fadd_rn(hi, b);
+  const float v = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(b, v));
+  const float t = __fadd_rn(e, lo);
+  rh = __fadd_rn(s, t);
+  rl = __fsub_rn(t, __fsub_rn(rh, s));
+}
+
+__device__ __forceinline__ double ff_pack(float hi, float lo) {
+  return __hiloint2double(__float_as_int(lo), __float_as_int(hi));
+}
+__device__ __forceinline__ float ff_hi(double d) { return __int_as_float(__double2loint(d)); }
+__device__ __forceinline__ float ff_lo(double d) { return __int_as_float(__double2hiint(d)); }
+
+template <typename Real>
+__device__ __forceinline__ double real_to_f64(Real k) {
+  if constexpr (sizeof(Real) == 8)
+    return k;
+  else
+    return f32_to_f64(k);
+}
+
+// One value: `a` is the accumulator slot (FP64 or float-float), k the
+// operator value; returns the next stage input (xn) and the new slot (an).
+template <int EPI, typename Real, typename OutT>
+__device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k, OutT& xn,
+                                          double& an) {
+  xn = OutT(0);
+  if constexpr (EPI == EPI_APPLY) {
+    an = real_to_f64<Real>(k);
+  } else if constexpr (EPI == EPI_F64_MID) {
+    const double x = a + sd.f1 * k;
+    xn = static_cast<OutT>(x);
+    an = x + sd.f2 * k;
+  } else if constexpr (EPI == EPI_F64_LAST) {
+    an = a + sd.f1 * k;
+  } else if constexpr (EPI == EPI_MIX_S1) {
+    const float ah = f64_to_f32(a);
+    const float al = f64_to_f32(a - f32_to_f64(ah));
+    xn = static_cast<OutT>(fmaf(sd.f1f, k, ah));
+    float rh, rl;
+    ff_add(ah, al, fmaf(sd.fb_hi, k, sd.fb_lo * k), rh, rl);
+    an = ff_pack(rh, rl);
+  } else if constexpr (EPI == EPI_MIX_MID) {
+    const float ah = ff_hi(a), al = ff_lo(a);
+    xn = static_cast<OutT>(fmaf(sd.f1f, k, ah));
+    float rh, rl;
+    ff_add(ah, al, fmaf(sd.fb_hi, k, sd.fb_lo * k), rh, rl);
+    an = ff_pack(rh, rl);
+  } else if constexpr (EPI == EPI_MIX_LAST) {
+    float rh, rl;
+    ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
+    an = f32_to_f64(rh) + f32_to_f64(rl);
+  } else {  // EPI_MIX_UPD
+    an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
   }
 }
 
@@ -252,12 +328,13 @@ __device__ __forceinline__ void store2(double* p, double a, double b) {
 struct CartArgs {
   LaunchArgs la;
   int32_t stage_x;  // X staged in shared memory (else read from A's buffer: X == A)
-  int32_t stage_a;  // A staged (RK modes)
   int32_t tma;      // bulk copies usable (alignment checked on the host)
 };
 
-template <int DIM, int NP, typename Real, typename InT, typename OutT>
+template <int DIM, int NP, typename Real, typename InT, int EPI>
 __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
+  using OutT = std::conditional_t<sizeof(Real) == 8, double, float>;
+  constexpr bool stage_a = EpiTraits<EPI>::stage_a;
   constexpr int N = ipow_c(NP, DIM);
   constexpr int F = DIM + 1;
   constexpr int NL = ipow_c(NP, DIM - 1);
@@ -265,7 +342,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   const LaunchArgs& La = ca.la;
   const int CB = La.cells_per_block;
   extern __shared__ __align__(128) unsigned char smem_cart[];
-  const CartSmem<DIM, NP, Real, InT> lay(CB, ca.stage_x != 0, ca.stage_a != 0);
+  const CartSmem<DIM, NP, Real, InT> lay(CB, ca.stage_x != 0, stage_a);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_cart + lay.bar);
   const size_t xstride = (size_t)((lay.xbytes + 127) & ~127);
   const size_t astride = (size_t)((lay.abytes + 127) & ~127);
@@ -276,21 +353,72 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
     return;
   }
   const CartBasis<Real>& B = CartConst<Real>::get();
-  const bool stage_x = ca.stage_x != 0, stage_a = ca.stage_a != 0;
+  const bool stage_x = (sizeof(InT) == 4) || ca.stage_x != 0;
 
   // issue the copies of work item w into buffer b
   auto issue = [&](int w, int b) {
     const WorkItem wi = La.work[w];
-    const SolveDesc& sd = La.solves ? La.solves[wi.solve] : La.single;
+    const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
+    const void* Xg = sdp->X;
+    const double* Ag = sdp->A;
     const size_t c0 = (size_t)wi.cell_begin * F * N;
     const uint32_t nx = (uint32_t)(wi.n_cells * F * N * sizeof(InT));
     const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
     uint32_t tx = 0;
     if (stage_x) tx += nx;
-    if (stage_a) tx += na;
+    if constexpr (stage_a) tx += na;
     mbar_expect_tx(&bars[b], tx);
-    if (stage_x) bulk_g2s(smem_cart + lay.X + b * xstride, static_cast<const InT*>(sd.X) + c0, nx, &bars[b]);
-    if (stage_a) bulk_g2s(smem_cart + lay.A + b * astride, sd.A + c0, na, &bars[b]);
+    if (stage_x) bulk_g2s(smem_cart + lay.X + b * xstride, static_cast<const InT*>(Xg) + c0, nx, &bars[b]);
+    if constexpr (stage_a) bulk_g2s(smem_cart + lay.A + b * astride, Ag + c0, na, &bars[b]);
+  };
+
+  // line task of this thread: (cell, direction, line), the same for every item
+  const int tcl = threadIdx.x / (DIM * NL);
+  const int te = (threadIdx.x - tcl * DIM * NL) / NL;
+  const int tt = threadIdx.x - tcl * DIM * NL - te * NL;
+  int tbase = 0;
+  {
+    int ti[3] = {0, 0, 0};
+    tbase = face_base<DIM, NP>(te, tt, ti);
+  }
+  const int tstr = dir_stride(te, NP);
+  // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
+  InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
+  const int nstride = blockDim.x;
+  // Neighbour lines (u_e and p, both sides) of item w that are not in the
+  // item's own block: asynchronous copies from L2 into this thread's slot.
+  auto prefetch_nb = [&](int w, int* nbs) {
+    nbs[0] = nbs[1] = -EW_BC_HARD_WALL_ID;
+    if (w < La.n_work) {
+      const WorkItem wi = La.work[w];
+      const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
+      const int32_t* nbr = sdp->nbr;
+      const int64_t ncells = sdp->n_cells;
+      const InT* Xg = static_cast<const InT*>(sdp->X);
+      if (tcl < wi.n_cells) {
+        const int cell = wi.cell_begin + tcl;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          int nb = nbr[(size_t)cell * 2 * DIM + 2 * te + s];
+          if (nb >= ncells) {
+            atomicOr(La.err, ERR_BAD_NEIGHBOR);
+            nb = cell;
+          }
+          nbs[s] = nb;
+          const int nl = nb - wi.cell_begin;
+          if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
+            const InT* xn = Xg + (size_t)nb * F * N;
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+              cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, xn + te * N + tbase + j * tstr);
+              cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride,
+                                    xn + DIM * N + tbase + j * tstr);
+            }
+          }
+        }
+      }
+    }
+    cp_async_commit();
   };
 
   if (threadIdx.x == 0) {
@@ -300,13 +428,16 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   }
   __syncthreads();
   if (ca.tma && threadIdx.x == 0 && (int)blockIdx.x < La.n_work) issue(blockIdx.x, 0);
+  int nbs[2];
 
   uint32_t phase = 0;  // bit b: parity of the next wait on buffer b
   int it = 0;
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
     const int b = it & 1;
     const WorkItem wi = La.work[w];
-    const SolveDesc& sd = La.solves ? La.solves[wi.solve] : La.single;
+    // by value: the fields live in registers instead of being re-read after
+    // every store (a reference could alias the output arrays)
+    const SolveDesc sd = La.solves ? La.solves[wi.solve] : La.single;
     const int nc = wi.n_cells;
     InT* sX = reinterpret_cast<InT*>(smem_cart + lay.X + b * xstride);
     double* sA = reinterpret_cast<double*>(smem_cart + lay.A + b * astride);
@@ -315,58 +446,29 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
       const Real* gc = static_cast<const Real*>(sd.cellc) + (size_t)wi.cell_begin * kCellConsts;
       for (int i = threadIdx.x; i < nc * kCellConsts; i += blockDim.x) sCell[i] = load_nc(gc + i);
     }
-    // line task of this thread and the traces of its non-local neighbours
-    // (read from L2 while the bulk copies are in flight)
-    const int task = threadIdx.x;
-    const int tcl = task / (DIM * NL);
-    const int te = (task - tcl * DIM * NL) / NL;
-    const int tt = task - tcl * DIM * NL - te * NL;
     const bool tactive = tcl < nc;
-    int tbase = 0;
-    {
-      int ti[3] = {0, 0, 0};
-      tbase = face_base<DIM, NP>(te, tt, ti);
-    }
-    const int tstr = dir_stride(te, NP);
-    int nbs[2] = {-EW_BC_HARD_WALL_ID, -EW_BC_HARD_WALL_ID};
-    Real nvu[2] = {Real(0), Real(0)}, nvp[2] = {Real(0), Real(0)};
-    if (tactive) {
-      const int cell = wi.cell_begin + tcl;
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        int nb = sd.nbr[(size_t)cell * 2 * DIM + 2 * te + s];
-        if (nb >= sd.n_cells) {
-          atomicOr(La.err, ERR_BAD_NEIGHBOR);
-          nb = cell;
-        }
-        nbs[s] = nb;
-        const int nl = nb - wi.cell_begin;
-        if (nb >= 0 && !(nl >= 0 && nl < nc)) {
-          const InT* xn = static_cast<const InT*>(sd.X) + (size_t)nb * F * N;
-          Real vu = Real(0), vp = Real(0);
-#pragma unroll
-          for (int j = 0; j < NP; ++j) {
-            const Real l = B.L[1 - s][j];
-            vu += l * to_real<Real>(load_nc(xn + te * N + tbase + j * tstr));
-            vp += l * to_real<Real>(load_nc(xn + DIM * N + tbase + j * tstr));
-          }
-          nvu[s] = vu;
-          nvp[s] = vp;
-        }
-      }
-    }
+    // this item's non-local neighbour lines: in flight during the bulk-copy
+    // wait and the own-line contractions, awaited just before the fluxes
+    prefetch_nb(w, nbs);
     if (ca.tma) {
       // prefetch the next item into the other buffer (its previous contents
       // were consumed before the end-of-item barrier of the last iteration)
-      if (threadIdx.x == 0 && w + (int)gridDim.x < La.n_work) {
+      const bool has_next = w + (int)gridDim.x < La.n_work;
+      if (threadIdx.x == 0 && has_next) {
         fence_proxy_async();
         issue(w + gridDim.x, b ^ 1);
       }
       const bool ok = mbar_wait(&bars[b], (phase >> b) & 1u);
       phase ^= (1u << b);
       if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicOr(La.err, ERR_WAIT_TIMEOUT);
-        continue;
+        // give up on this CTA's remaining items: wait (bounded) for the
+        // copies still in flight, then leave
+        if (threadIdx.x == 0) {
+          atomicOr(La.err, ERR_WAIT_TIMEOUT);
+          if (has_next) mbar_wait(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+        }
+        cp_async_wait_all();
+        break;
       }
     } else {
       const size_t c0 = (size_t)wi.cell_begin * F * N;
@@ -374,7 +476,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
         const InT* gx = static_cast<const InT*>(sd.X) + c0;
         for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sX[i] = gx[i];
       }
-      if (stage_a) {
+      if constexpr (stage_a) {
         const double* ga = sd.A + c0;
         for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sA[i] = ga[i];
       }
@@ -384,8 +486,12 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
     // ---------------------------------------------------------- line phase
     // stage input values as Real, from the X buffer or (X == A) the A buffer
     auto xval = [&](int idx) -> Real {
-      if (stage_x) return to_real<Real>(sX[idx]);
-      return to_real<Real>(sA[idx]);
+      if constexpr (sizeof(InT) == 4) {
+        return sX[idx];
+      } else {
+        const double* src = stage_x ? reinterpret_cast<const double*>(sX) : sA;
+        return to_real<Real>(src[idx]);
+      }
     };
     const Real bf = static_cast<Real>(sd.bf);
     {
@@ -422,6 +528,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
         }
         const Real tu[2] = {su + au, su - au};
         const Real tp[2] = {sp + ap, sp - ap};
+        cp_async_wait_all();  // this thread's neighbour lines
         // fluxes at both ends (without the face JxW)
         Real Fu[2], Fp[2];
 #pragma unroll
@@ -432,12 +539,18 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
           Real lambda;
           if (nb >= 0) {
             const int nl = nb - wi.cell_begin;
-            Real vu = nvu[s], vp = nvp[s];
-            if (nl >= 0 && nl < nc) {
+            Real vu = Real(0), vp = Real(0);
+            if (!(nl >= 0 && nl < nc)) {
+              // neighbour's line from this thread's prefetch slot
+#pragma unroll
+              for (int j = 0; j < NP; ++j) {
+                const Real l = B.L[1 - s][j];
+                vu += l * to_real<Real>(nslot[((2 * s) * NP + j) * nstride]);
+                vp += l * to_real<Real>(nslot[((2 * s + 1) * NP + j) * nstride]);
+              }
+            } else {
               // neighbour in this block: its trace on the opposite face, l_j(1-s)
               const int no = nl * F * N;
-              vu = Real(0);
-              vp = Real(0);
 #pragma unroll
               for (int j = 0; j < NP; ++j) {
                 const Real l = B.L[1 - s][j];
@@ -493,11 +606,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
         // finish u_e on this line (x-lines are contiguous: paired stores)
         const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + e * N + base;
         const int l0 = xo + e * N + base;
-        const int mode = sd.mode;
-        if (mode == MODE_APPLY) {
-#pragma unroll
-          for (int i = 0; i < NP; ++i) sd.Aout[g0 + i * str] = static_cast<double>(ku[i]);
-        } else {
+        {
           const bool paired = NP % 2 == 0 && e == 0 &&
                               (reinterpret_cast<uintptr_t>(sd.Aout) & 15) == 0 &&
                               (reinterpret_cast<uintptr_t>(sd.Xout) & 7) == 0;
@@ -505,20 +614,17 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
           for (int i = 0; i < NP; i += 2) {
             OutT x0, x1 = OutT(0);
             double a0, a1 = 0.0;
-            const double aa = stage_a ? sA[l0 + i * str] : sd.A[g0 + i * str];
-            update_point<Real, OutT>(sd, mode, aa, ku[i], x0, a0);
-            if (i + 1 < NP) {
-              const double ab = stage_a ? sA[l0 + (i + 1) * str] : sd.A[g0 + (i + 1) * str];
-              update_point<Real, OutT>(sd, mode, ab, ku[i + 1], x1, a1);
-            }
+            epi_value<EPI, Real, OutT>(sd, stage_a ? sA[l0 + i * str] : 0.0, ku[i], x0, a0);
+            if (i + 1 < NP)
+              epi_value<EPI, Real, OutT>(sd, stage_a ? sA[l0 + (i + 1) * str] : 0.0, ku[i + 1], x1, a1);
             if (paired) {
-              if (mode == MODE_RK_MID) store2(static_cast<OutT*>(sd.Xout) + g0 + i, x0, x1);
+              if constexpr (EpiTraits<EPI>::writes_x) store2(static_cast<OutT*>(sd.Xout) + g0 + i, x0, x1);
               store2(sd.Aout + g0 + i, a0, a1);
             } else {
-              if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g0 + i * str] = x0;
+              if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g0 + i * str] = x0;
               sd.Aout[g0 + i * str] = a0;
               if (i + 1 < NP) {
-                if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g0 + (i + 1) * str] = x1;
+                if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g0 + (i + 1) * str] = x1;
                 sd.Aout[g0 + (i + 1) * str] = a1;
               }
             }
@@ -541,17 +647,11 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
       if (cl == src_local) k += src_val * static_cast<const Real*>(sd.src_w)[q];
       const size_t g = ((size_t)wi.cell_begin + cl) * F * N + DIM * N + q;
       const int lidx = cl * F * N + DIM * N + q;
-      const int mode = sd.mode;
-      if (mode == MODE_APPLY) {
-        sd.Aout[g] = static_cast<double>(k);
-      } else {
-        const double a = stage_a ? sA[lidx] : sd.A[g];
-        OutT xn;
-        double an;
-        update_point<Real, OutT>(sd, mode, a, k, xn, an);
-        if (mode == MODE_RK_MID) static_cast<OutT*>(sd.Xout)[g] = xn;
-        sd.Aout[g] = an;
-      }
+      OutT xn;
+      double an;
+      epi_value<EPI, Real, OutT>(sd, stage_a ? sA[lidx] : 0.0, k, xn, an);
+      if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
+      sd.Aout[g] = an;
     }
     __syncthreads();
   }

@@ -72,20 +72,18 @@ struct CkK {
   }
 };
 
-template <typename Real, typename InT, typename OutT>
+template <typename Real, typename InT, int EPI>
 struct CartK {
-  static size_t smem(int cb, int sx, int sa) {
-    return CartSmem<DIM, NP, Real, InT>(cb, sx != 0, sa != 0).end;
-  }
-  static cudaError_t launch(const LaunchArgs& a, int sx, int sa, int tma, int grid, cudaStream_t st) {
+  static constexpr bool SA = EpiTraits<EPI>::stage_a;
+  static size_t smem(int cb, int sx) { return CartSmem<DIM, NP, Real, InT>(cb, sx != 0, SA).end; }
+  static cudaError_t launch(const LaunchArgs& a, int sx, int tma, int grid, cudaStream_t st) {
     CartArgs ca;
     ca.la = a;
     ca.stage_x = sx;
-    ca.stage_a = sa;
     ca.tma = tma;
     const int cb = a.cells_per_block;
-    const size_t sm = smem(cb, sx, sa);
-    auto kern = stage_cart_kernel<DIM, NP, Real, InT, OutT>;
+    const size_t sm = smem(cb, sx);
+    auto kern = stage_cart_kernel<DIM, NP, Real, InT, EPI>;
     carveout(kern);
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -94,9 +92,9 @@ struct CartK {
     kern<<<grid, cb * DIM * ipow_c(NP, DIM - 1), sm, st>>>(ca);
     return cudaGetLastError();
   }
-  static int occupancy(int cb, int sx, int sa) {
-    return blocks_per_sm(stage_cart_kernel<DIM, NP, Real, InT, OutT>, cb * DIM * ipow_c(NP, DIM - 1),
-                         smem(cb, sx, sa));
+  static int occupancy(int cb, int sx) {
+    return blocks_per_sm(stage_cart_kernel<DIM, NP, Real, InT, EPI>, cb * DIM * ipow_c(NP, DIM - 1),
+                         smem(cb, sx));
   }
 };
 
@@ -134,9 +132,15 @@ void EW_TABLE_FN(KernelTable& t) {
   t.points = N;
   t.lines = DIM * ipow_c(NP, DIM - 1);
   t.set_constants = &set_constants;
-  fill_cart<CartK<double, double, double>>(t.cart[STAGE_F64]);
-  fill_cart<CartK<float, double, float>>(t.cart[STAGE_MIX_IN64]);
-  fill_cart<CartK<float, float, float>>(t.cart[STAGE_MIX_IN32]);
+  fill_cart<CartK<double, double, EPI_APPLY>>(t.cart[CV_F64_APPLY]);
+  fill_cart<CartK<double, double, EPI_F64_MID>>(t.cart[CV_F64_MID]);
+  fill_cart<CartK<double, double, EPI_F64_LAST>>(t.cart[CV_F64_LAST]);
+  fill_cart<CartK<float, double, EPI_APPLY>>(t.cart[CV_MIX_APPLY64]);
+  fill_cart<CartK<float, double, EPI_MIX_S1>>(t.cart[CV_MIX_S1]);
+  fill_cart<CartK<float, float, EPI_APPLY>>(t.cart[CV_MIX_APPLY32]);
+  fill_cart<CartK<float, float, EPI_MIX_MID>>(t.cart[CV_MIX_MID]);
+  fill_cart<CartK<float, float, EPI_MIX_LAST>>(t.cart[CV_MIX_LAST]);
+  fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);

@@ -20,6 +20,9 @@ int validate_mesh(const ew_mesh_desc* m, bool* cartesian, std::string* err);
 // current device.
 cudaError_t upload_cart_constants(int dim, int np);
 
+// Tuned cells per block for (dim, degree, precision); 0 when unset.
+int tuned_cells_per_block(int dim, int degree, int precision);
+
 // LowStorageRK45Reg2 coefficients (time_integrators.cc:243-252)
 constexpr double kA21 = 970286171893. / 4311952581923.;
 constexpr double kA32 = 6584761158862. / 12103376702013.;

@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
 
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
     const WorkItem wi = La.work[w];
-    const SolveDesc& sd = pick(La, wi.solve);
+    const SolveDesc sd = pick(La, wi.solve);  // by value: no reloads after stores
     const int nc = wi.n_cells;
     __syncthreads();  // previous item done with shared memory; basis loaded
     load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
@@ -402,33 +402,29 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
     const int mode = sd.mode;
     if (mode == MODE_APPLY) {
 #pragma unroll
-      for (int fld = 0; fld < F; ++fld) sd.Aout[g0 + fld * N] = static_cast<double>(k[fld]);
-    } else if (mode == MODE_RK_MID) {
-      OutT* Xo = static_cast<OutT*>(sd.Xout);
+      for (int fld = 0; fld < F; ++fld) {
+        if constexpr (sizeof(Real) == 8)
+          sd.Aout[g0 + fld * N] = k[fld];
+        else
+          sd.Aout[g0 + fld * N] = f32_to_f64(k[fld]);
+      }
+    } else {
+      // one FP64 operation per value whatever the mode (a data-independent
+      // select of the coefficients, so nothing is if-converted twice)
+      const bool mid = mode == MODE_RK_MID;
 #pragma unroll
       for (int fld = 0; fld < F; ++fld) {
         const size_t g = g0 + fld * N;
         const double a = sd.A[g];
         if constexpr (sizeof(Real) == 8) {
           const double xn = a + sd.f1 * k[fld];
-          Xo[g] = static_cast<OutT>(xn);
-          sd.Aout[g] = xn + sd.f2 * k[fld];
+          if (mid) static_cast<OutT*>(sd.Xout)[g] = static_cast<OutT>(xn);
+          sd.Aout[g] = fma(mid ? sd.f2 : 0.0, k[fld], xn);
         } else {
           const float kf = k[fld];
-          Xo[g] = static_cast<OutT>(fmaf(sd.f1f, kf, f64_to_f32(a)));
-          sd.Aout[g] = a + f32_to_f64(fmaf(sd.fb_hi, kf, sd.fb_lo * kf));
-        }
-      }
-    } else {  // MODE_RK_LAST
-#pragma unroll
-      for (int fld = 0; fld < F; ++fld) {
-        const size_t g = g0 + fld * N;
-        const double a = sd.A[g];
-        if constexpr (sizeof(Real) == 8) {
-          sd.Aout[g] = a + sd.f1 * k[fld];
-        } else {
-          const float kf = k[fld];
-          sd.Aout[g] = a + f32_to_f64(fmaf(sd.f1_hi, kf, sd.f1_lo * kf));
+          if (mid) static_cast<OutT*>(sd.Xout)[g] = static_cast<OutT>(fmaf(sd.f1f, kf, f64_to_f32(a)));
+          const float ch = mid ? sd.fb_hi : sd.f1_hi, cl2 = mid ? sd.fb_lo : sd.f1_lo;
+          sd.Aout[g] = a + f32_to_f64(fmaf(ch, kf, cl2 * kf));
         }
       }
     }
@@ -587,7 +583,7 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
 
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
     const WorkItem wi = La.work[w];
-    const SolveDesc& sd = pick(La, wi.solve);
+    const SolveDesc sd = pick(La, wi.solve);  // by value: no reloads after stores
     const int nc = wi.n_cells;
     __syncthreads();
     load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);

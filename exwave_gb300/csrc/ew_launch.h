@@ -22,19 +22,33 @@ struct KernelEntry {
   size_t (*smem)(int cells_per_block) = nullptr;
 };
 
-// Launcher of the Cartesian line kernel (ew_cart.cuh).
+// Variants of the Cartesian line kernel (ew_cart.cuh): compute precision,
+// input type and epilogue.
+enum CartVariant : int {
+  CV_F64_APPLY = 0,   // FP64: dst = M^-1 A(X)
+  CV_F64_MID = 1,     // FP64 LSRK stage 1..4
+  CV_F64_LAST = 2,    // FP64 LSRK stage 5 / ADER update
+  CV_MIX_APPLY64 = 3, // FP32 operator on an FP64 input: dst = M^-1 A(X)
+  CV_MIX_S1 = 4,      // mixed LSRK stage 1 (FP64 state in)
+  CV_MIX_APPLY32 = 5, // FP32 operator on an FP32 input
+  CV_MIX_MID = 6,     // mixed LSRK stages 2..4
+  CV_MIX_LAST = 7,    // mixed LSRK stage 5 (FP64 state out)
+  CV_MIX_UPD = 8,     // mixed ADER update u + M^-1 A(T)
+  N_CART_VARIANTS = 9
+};
+
+// Launcher of the Cartesian line kernel.
 struct CartEntry {
-  cudaError_t (*launch)(const LaunchArgs&, int stage_x, int stage_a, int tma, int grid,
-                        cudaStream_t) = nullptr;
-  int (*occupancy)(int cells_per_block, int stage_x, int stage_a) = nullptr;
-  size_t (*smem)(int cells_per_block, int stage_x, int stage_a) = nullptr;
+  cudaError_t (*launch)(const LaunchArgs&, int stage_x, int tma, int grid, cudaStream_t) = nullptr;
+  int (*occupancy)(int cells_per_block, int stage_x) = nullptr;
+  size_t (*smem)(int cells_per_block, int stage_x) = nullptr;
 };
 
 struct KernelTable {
   int dim = 0, np = 0, points = 0;
   int lines = 0;  // threads per cell of the Cartesian kernel: dim * np^(dim-1)
   KernelEntry stage[N_STAGE_VARIANTS][2];  // [variant][cartesian]
-  CartEntry cart[N_STAGE_VARIANTS];
+  CartEntry cart[N_CART_VARIANTS];
   KernelEntry ck[2][2][2];                 // [mixed][cartesian][post]
   // upload the even-odd 1D constants of this degree to the current device
   cudaError_t (*set_constants)(const double* w, const double* D, const double* L0,

@@ -233,6 +233,13 @@ int ew_batch_set_stream(ew_batch* batch, void* stream);
 int ew_batch_synchronize(ew_batch* batch);
 int64_t ew_batch_kernel_launches(const ew_batch* batch);
 
+/* Tuning table consulted by ew_create (when options->cells_per_block is 0)
+ * and by the batch runtime: cells per thread block of the operator kernel
+ * for (dim, degree, precision); 0 restores the built-in default.  Written by
+ * the autotuner (exwave_gb300/autotune.py).  No reference counterpart. */
+int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_per_block);
+int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision);
+
 /* Waits for the context's stream and reports a raised device error flag. */
 int ew_synchronize(ew_ctx* ctx);
 
