@@ -847,6 +847,83 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
   return EW_OK;
 }
 
+// ---- LSRK45 step with its scratch in a static device array ------------------
+namespace {
+// Stage scratch of ew_lsrk45_step_static (two FP32 stage inputs, or the FP64
+// third register); held by every device that loads the library.
+__device__ __align__(256) float g_static_scratch[EW_STATIC_SCRATCH_BYTES / sizeof(float)];
+constexpr int kMaxDevices = 64;
+float* g_static_ptr[kMaxDevices] = {};
+std::mutex g_static_mutex;
+
+// Device address of the array on the current device (looked up once per device).
+int static_scratch(ew_ctx* c, float** out) {
+  std::lock_guard<std::mutex> lk(g_static_mutex);
+  if (c->device < 0 || c->device >= kMaxDevices)
+    return fail(c, EW_ERR_INVALID, "device ordinal too large for the static scratch table");
+  if (!g_static_ptr[c->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(c, e, "cudaGetSymbolAddress(static scratch)");
+    g_static_ptr[c->device] = static_cast<float*>(p);
+  }
+  *out = g_static_ptr[c->device];
+  return EW_OK;
+}
+}  // namespace
+
+int ew_lsrk45_step_static(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step_static: vec_n and vec_np must be distinct");
+  if (ctx->n_dofs > EW_STATIC_SCRATCH_MAX_DOFS)
+    return fail(ctx, EW_ERR_TOO_LARGE,
+                "ew_lsrk45_step_static: " + std::to_string(ctx->n_dofs) +
+                    " DoFs exceed the static scratch (at most " +
+                    std::to_string((long long)EW_STATIC_SCRATCH_MAX_DOFS) + " DoFs)");
+  float* scratch = nullptr;
+  if ((rc = static_scratch(ctx, &scratch))) return rc;
+  using namespace ew;
+  const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
+  const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
+                        0.0};
+  if (!ctx->mixed) {
+    // FP64: the third register of the two-register scheme lives in the array
+    double* N = vec_n;
+    double* P = vec_np;
+    double* T = reinterpret_cast<double*>(scratch);
+    struct S {
+      const double* X;
+      const double* A;
+      double* Xo;
+      double* Ao;
+    } st[5] = {{N, N, T, P}, {T, P, P, N}, {P, N, N, T}, {N, T, T, P}, {T, P, nullptr, P}};
+    for (int s = 0; s < 5; ++s) {
+      rc = launch_stage(ctx, STAGE_F64, s < 4 ? CV_F64_MID : CV_F64_LAST, st[s].A, st[s].X,
+                        st[s].Xo, st[s].Ao, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+      if (rc) return rc;
+    }
+    return EW_OK;
+  }
+  // mixed: the two FP32 stage inputs live in the array (second one at a
+  // 256-byte aligned offset)
+  const size_t off = ((size_t)ctx->n_dofs + 63) & ~(size_t)63;
+  float* X0 = scratch;
+  float* X1 = scratch + off;
+  rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0],
+                    f2[0], 1.0f);
+  if (rc) return rc;
+  const float* xin[4] = {X0, X1, X0, X1};
+  float* xout[4] = {X1, X0, X1, nullptr};
+  for (int s = 1; s < 5; ++s) {
+    rc = launch_stage(ctx, STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1],
+                      xout[s - 1], vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
+    if (rc) return rc;
+  }
+  return EW_OK;
+}
+
 int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst) {
   int rc = check(ctx);
   if (rc) return rc;

@@ -116,6 +116,25 @@ int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const doubl
  * the reference. */
 int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
 
+/* The same LSRK45 step as ew_lsrk45_step, for callers that cannot have the
+ * library allocate device memory: it has no counterpart in the reference.
+ * Code that runs the step inside an application which owns all device
+ * memory through its own pool or a fixed budget, or inside a
+ * latency-sensitive loop, cannot use cudaMalloc there (it synchronises the
+ * device and fails when the pool holds the memory).  This entry point keeps
+ * its stage scratch in one static device array of EW_STATIC_SCRATCH_BYTES
+ * (64 MiB) that every GPU loading the library holds until exit, and calls no
+ * allocator.  Limit: n_dofs <= EW_STATIC_SCRATCH_MAX_DOFS, larger contexts
+ * get EW_ERR_TOO_LARGE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls on a device share the
+ * array and it keeps the last call's contents (every stage writes the
+ * scratch it later reads, so nothing has to start at zero): calls that
+ * overlap on the GPU race. */
+#define EW_STATIC_SCRATCH_BYTES (64ll << 20)
+#define EW_STATIC_SCRATCH_MAX_DOFS ((EW_STATIC_SCRATCH_BYTES / 8) - 64)
+int ew_lsrk45_step_static(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
+
 /* Replaces WaveEquationOperationADER::apply_ader (wave_equation_operations.cc:1346-1381):
  * T = Taylor time integral of src over [0,dt]; dst = -M^{-1} A(T). */
 int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst);
