@@ -560,6 +560,20 @@ int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
   a.single.X = src;
   a.single.Xout = T;
   a.dt = dt;
+  // Taylor coefficients (integrate_taylor_cauchykovalewski_step,
+  // wave_equation_operations.cc:1079-1082): fac_s = -1/2 prod_{j=2}^{s+2}
+  // (-1/(j+1)), times dt^(s+3)
+  a.ck_dt_d = dt;
+  a.ck_half_dt2_d = 0.5 * dt * dt;
+  a.ck_dt = (float)dt;
+  a.ck_half_dt2 = (float)(0.5 * dt * dt);
+  double fac = -0.5, dtp = dt * dt * dt;
+  for (int s = 0; s < 8; ++s) {
+    fac /= -(s + 3.0);
+    a.ck_fac_d[s] = fac * dtp;
+    a.ck_fac[s] = (float)(fac * dtp);
+    dtp *= dt;
+  }
   const ew::KernelEntry& k = c->kt->ck[c->mixed ? 1 : 0][c->cart ? 1 : 0][c->post ? 1 : 0];
   cudaError_t e = k.launch(a, c->grid_ck, c->stream);
   ++c->launches;

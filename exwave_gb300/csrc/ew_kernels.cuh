@@ -432,108 +432,88 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
 }
 
 // ============================================================ CK kernel
-// One sweep of a 1D matrix M (rows x cols) along direction e over the
-// tensors of nc cells x F fields.  in/out: [cell][field][points] with
-// per-cell stride cs and per-field stride equal to the tensor size.
-template <int DIM, typename Real>
-__device__ __forceinline__ void sweep(const Real* M, int rows, int cols, int e, const int* ext_in,
-                                      const Real* in, int cs_in, Real* out, int cs_out, int nc,
-                                      int nfields) {
-  int ext_out[3] = {ext_in[0], ext_in[1], ext_in[2]};
-  ext_out[e] = rows;
-  int tin = 1, tout = 1;
-  for (int d = 0; d < DIM; ++d) {
-    tin *= ext_in[d];
-    tout *= ext_out[d];
-  }
-  const int total = nc * nfields * tout;
-  const int str_in = (e == 0) ? 1 : (e == 1 ? ext_in[0] : ext_in[0] * ext_in[1]);
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int cl = idx / (nfields * tout);
-    const int r = idx - cl * nfields * tout;
-    const int fld = r / tout;
-    const int p = r - fld * tout;
-    int o[3] = {0, 0, 0};
-    {
-      int tt = p;
-      for (int d = 0; d < DIM; ++d) {
-        o[d] = tt % ext_out[d];
-        tt /= ext_out[d];
-      }
-    }
-    int base = 0, str = 1;
-    for (int d = 0; d < DIM; ++d) {
-      if (d != e) base += o[d] * str;
-      str *= ext_in[d];
-    }
-    const Real* src = in + cl * cs_in + fld * tin + base;
-    const Real* mrow = M + o[e] * cols;
+// One sweep of a 1D matrix Mtx (ROWS x COLS, COLS = input extent along DIR)
+// along direction DIR over the tensors of nc cells x nf fields; input
+// extents I0 x I1 x I2, compile-time, per-cell strides cs_in / cs_out.
+template <int DIM, typename Real, int DIR, int ROWS, int I0, int I1, int I2>
+__device__ __forceinline__ void sweep_ct(const Real* Mtx, const Real* in, int cs_in, Real* out,
+                                         int cs_out, int nc, int nf) {
+  constexpr int O0 = DIR == 0 ? ROWS : I0;
+  constexpr int O1 = DIR == 1 ? ROWS : I1;
+  constexpr int O2 = DIR == 2 ? ROWS : I2;
+  constexpr int TIN = I0 * (DIM > 1 ? I1 : 1) * (DIM > 2 ? I2 : 1);
+  constexpr int TOUT = O0 * (DIM > 1 ? O1 : 1) * (DIM > 2 ? O2 : 1);
+  constexpr int COLS = DIR == 0 ? I0 : (DIR == 1 ? I1 : I2);
+  constexpr int SIN = DIR == 0 ? 1 : (DIR == 1 ? I0 : I0 * I1);
+  for (int idx = threadIdx.x; idx < nc * nf * TOUT; idx += blockDim.x) {
+    const int cf = idx / TOUT;  // cell * nf + field
+    const int p = idx - cf * TOUT;
+    const int cl = cf / nf;
+    const int fld = cf - cl * nf;
+    const int o0 = p % O0;
+    const int o1 = DIM > 1 ? (p / O0) % O1 : 0;
+    const int o2 = DIM > 2 ? p / (O0 * O1) : 0;
+    const int base = (DIR == 0 ? 0 : o0) + (DIR == 1 ? 0 : o1 * I0) + (DIR == 2 ? 0 : o2 * I0 * I1);
+    const int od = DIR == 0 ? o0 : (DIR == 1 ? o1 : o2);
+    const Real* src = in + cl * cs_in + fld * TIN + base;
+    const Real* mrow = Mtx + od * COLS;
     Real s = Real(0);
-    for (int j = 0; j < cols; ++j) s += mrow[j] * src[j * str_in];
-    out[cl * cs_out + fld * tout + p] = s;
+#pragma unroll
+    for (int j = 0; j < COLS; ++j) s += mrow[j] * src[j * SIN];
+    out[cl * cs_out + fld * TOUT + p] = s;
   }
 }
 
-// Apply a 1D matrix in all DIM directions (rows x cols per direction).
-// Result lands in `dst` (which may alias `src` only when DIM sweeps end
-// there); t1, t2 are scratch.  Contains __syncthreads.
-template <int DIM, typename Real>
-__device__ __forceinline__ void tensor_all(const Real* M, int rows, int cols, const Real* src,
-                                           int cs_src, Real* dst, int cs_dst, Real* t1, Real* t2,
-                                           int cs_t, int nc, int nfields) {
-  int ext[3] = {cols, cols, cols};
+// A 1D matrix (ROWS x COLS) applied in all DIM directions: src (COLS^DIM
+// points) -> dst (ROWS^DIM points); t1, t2 scratch.  Contains barriers.
+template <int DIM, typename Real, int ROWS, int COLS>
+__device__ __forceinline__ void tensor_ct(const Real* Mtx, const Real* src, int cs_src, Real* dst,
+                                          int cs_dst, Real* t1, Real* t2, int cs_t, int nc, int nf) {
   if constexpr (DIM == 2) {
-    sweep<DIM, Real>(M, rows, cols, 0, ext, src, cs_src, t1, cs_t, nc, nfields);
+    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, 1>(Mtx, src, cs_src, t1, cs_t, nc, nf);
     __syncthreads();
-    ext[0] = rows;
-    sweep<DIM, Real>(M, rows, cols, 1, ext, t1, cs_t, dst, cs_dst, nc, nfields);
+    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, 1>(Mtx, t1, cs_t, dst, cs_dst, nc, nf);
     __syncthreads();
   } else {
-    sweep<DIM, Real>(M, rows, cols, 0, ext, src, cs_src, t1, cs_t, nc, nfields);
+    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, COLS>(Mtx, src, cs_src, t1, cs_t, nc, nf);
     __syncthreads();
-    ext[0] = rows;
-    sweep<DIM, Real>(M, rows, cols, 1, ext, t1, cs_t, t2, cs_t, nc, nfields);
+    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, COLS>(Mtx, t1, cs_t, t2, cs_t, nc, nf);
     __syncthreads();
-    ext[1] = rows;
-    sweep<DIM, Real>(M, rows, cols, 2, ext, t2, cs_t, dst, cs_dst, nc, nfields);
+    sweep_ct<DIM, Real, 2, ROWS, ROWS, ROWS, COLS>(Mtx, t2, cs_t, dst, cs_dst, nc, nf);
     __syncthreads();
   }
 }
 
-// Derivative of the field set S (level r, m points per direction) at point
-// qq of cell cl: out_u_d = rho^{-1} d_d S_p, out_p = rho c^2 div S_u
+// Derivative of the field set S at level with M points per direction, at
+// point qq: out_u_d = rho^{-1} d_d S_p, out_p = rho c^2 div S_u
 // (integrate_taylor_cauchykovalewski_step, wave_equation_operations.cc:1096-1197).
-template <int DIM, int NP, typename Real, bool CART>
-__device__ __forceinline__ void ck_derivative(const Level<Real>& L, const Real* Sv, const Real* sGeo,
-                                              Real rho, Real c_sq, int qq, Real* out) {
-  using Sh = Shape<DIM, NP, CART>;
-  const int m = L.m;
-  int Nm = m;
-  for (int d = 1; d < DIM; ++d) Nm *= m;
+template <int DIM, int M, typename Real, bool CART>
+__device__ __forceinline__ void ck_deriv(const Real* D, const Real* x, const Real* Sv,
+                                         const Real* sGeo, Real rho, Real c_sq, int qq, Real* out) {
+  constexpr int NM = ipow_c(M, DIM);
   int i[3] = {0, 0, 0};
-  {
-    int t = qq;
-    for (int d = 0; d < DIM; ++d) {
-      i[d] = t % m;
-      t /= m;
-    }
-  }
+  i[0] = qq % M;
+  if constexpr (DIM > 1) i[1] = (qq / M) % M;
+  if constexpr (DIM > 2) i[2] = qq / (M * M);
   Real g[DIM + 1][DIM];
 #pragma unroll
   for (int fld = 0; fld <= DIM; ++fld) {
 #pragma unroll
     for (int e = 0; e < DIM; ++e) {
-      const int str = (e == 0) ? 1 : (e == 1 ? m : m * m);
-      const Real* row = L.D + i[e] * m;
-      const Real* line = Sv + fld * Nm + qq - i[e] * str;
+      constexpr int dummy = 0;
+      (void)dummy;
+      const int str = (e == 0) ? 1 : (e == 1 ? M : M * M);
+      const Real* row = D + i[e] * M;
+      const Real* line = Sv + fld * NM + qq - i[e] * str;
       Real s = Real(0);
-      for (int a = 0; a < m; ++a) s += row[a] * line[a * str];
+#pragma unroll
+      for (int a = 0; a < M; ++a) s += row[a] * line[a * str];
       g[fld][e] = s;
     }
   }
   Real xi[DIM];
 #pragma unroll
-  for (int e = 0; e < DIM; ++e) xi[e] = L.x[i[e]];
+  for (int e = 0; e < DIM; ++e) xi[e] = x[i[e]];
   Real JiT[DIM][DIM];
   cell_geom<DIM, Real, CART>(sGeo, xi, JiT);
   Real div = Real(0);
@@ -550,7 +530,88 @@ __device__ __forceinline__ void ck_derivative(const Level<Real>& L, const Real* 
     out[d] = rho_inv * pg;
   }
   out[DIM] = c_sq * rho * div;
-  (void)sizeof(Sh);
+}
+
+// Shared state of one CK work item.
+template <typename Real>
+struct CkState {
+  Real* sB;
+  Real* sS;
+  Real* sT1;
+  Real* sT2;
+  Real* sm;
+  const int* C;  // level contribution offsets (in units of Real)
+  const Real* sGeo;
+  int cl, q, nc;
+  bool active;
+  Real rho, c_sq;
+};
+
+// Recursive steps s = S..NSTEPS-1 of the Cauchy-Kovalevskaya procedure:
+// derivative j = s + 2 at level r = s/2 (M = NP - 2r points per direction),
+// added to the level's contribution; after odd steps the field set is
+// L2-projected onto the next lower level (degree - 2).
+template <int DIM, int NP, typename Real, bool CART, int S, int NSTEPS>
+__device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Real* c0) {
+  constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
+  constexpr int R = S / 2;
+  constexpr int M = NP - 2 * R;
+  constexpr int NM = ipow_c(M, DIM);
+  constexpr int GEO = CART ? DIM : (1 << DIM) * DIM;
+  const Level<Real> L = get_level(st.sB, NP, R);
+  Real sn[F];
+  const bool act = st.active && st.q < NM;
+  if (act)
+    ck_deriv<DIM, M, Real, CART>(L.D, L.x, st.sS + st.cl * F * N, st.sGeo + st.cl * GEO, st.rho,
+                                 st.c_sq, st.q, sn);
+  __syncthreads();
+  if (act) {
+    const Real f = fac[S];
+#pragma unroll
+    for (int fld = 0; fld < F; ++fld) {
+      st.sS[st.cl * F * N + fld * NM + st.q] = sn[fld];
+      if constexpr (R == 0)
+        c0[fld] += f * sn[fld];
+      else
+        st.sm[st.C[R] + st.cl * F * NM + fld * NM + st.q] += f * sn[fld];
+    }
+  }
+  __syncthreads();
+  if constexpr (S + 1 < NSTEPS) {
+    if constexpr (S % 2 == 1) {
+      const Level<Real> Ln = get_level(st.sB, NP, R + 1);
+      tensor_ct<DIM, Real, M - 2, M>(Ln.P, st.sS, F * N, st.sS, F * N, st.sT1, st.sT2, F * N, st.nc, F);
+    }
+    ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS>(st, fac, c0);
+  }
+}
+
+// Bottom-up: contribution of level R interpolated to level R-1 and added.
+template <int DIM, int NP, typename Real, int R>
+__device__ __forceinline__ void ck_gather(CkState<Real>& st, Real* c0) {
+  if constexpr (R >= 1) {
+    constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
+    constexpr int M = NP - 2 * R, MP = M + 2;
+    constexpr int NMP = ipow_c(MP, DIM);
+    const Level<Real> Lr = get_level(st.sB, NP, R);
+    Real* up = (DIM == 2) ? st.sT2 : st.sT1;
+    tensor_ct<DIM, Real, MP, M>(Lr.E, st.sm + st.C[R], F * ipow_c(M, DIM), up, F * N, st.sT1, st.sT2,
+                                F * N, st.nc, F);
+    if constexpr (R - 1 == 0) {
+      if (st.active) {
+#pragma unroll
+        for (int fld = 0; fld < F; ++fld) c0[fld] += up[st.cl * F * N + fld * NMP + st.q];
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < st.nc * F * NMP; idx += blockDim.x) {
+        const int c2 = idx / (F * NMP);
+        const int rr = idx - c2 * F * NMP;
+        st.sm[st.C[R - 1] + c2 * F * NMP + rr] += up[c2 * F * N + rr];
+      }
+    }
+    __syncthreads();
+    ck_gather<DIM, NP, Real, R - 1>(st, c0);
+  }
 }
 
 template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST>
@@ -558,6 +619,9 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
   using S = Shape<DIM, NP, CART>;
   constexpr int F = S::F, N = S::N;
   constexpr int NL = n_levels(NP);
+  // Taylor terms j = 0..max(k,2); derivatives j >= 2 come from the steps
+  constexpr int NSTEPS = (NP - 2 > 1) ? NP - 2 : 1;
+  constexpr int RLAST = (NSTEPS - 1) / 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real* sm = reinterpret_cast<Real*>(smem_raw);
   const int CB = La.cells_per_block;
@@ -568,27 +632,36 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
   Real* sFl = sm + lay.op.Fl;
   Real* sGeo = sm + lay.op.geo;
   Real* sMat = sm + lay.op.mat;
-  Real* sS = sm + lay.Sv;
-  Real* sT1 = sm + lay.T1;
-  Real* sT2 = sm + lay.T2;
   if ((int)blockDim.x != CB * N) {
     if (threadIdx.x == 0) atomicOr(La.err, ERR_BAD_LAUNCH);
     return;
   }
   load_basis<Real>(La.basis, sB, basis_total(NP));
-  const double dt = La.dt;
-  // Taylor terms j = 0..max(k,2); derivatives j >= 2 come from the
-  // recursive steps s = 0..n_steps-1.
-  const int n_steps = (NP - 2 > 1) ? NP - 2 : 1;
+  Real fac[8];
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    if constexpr (sizeof(Real) == 8)
+      fac[s] = La.ck_fac_d[s];
+    else
+      fac[s] = La.ck_fac[s];
+  }
+  Real dtr, half_dt2;
+  if constexpr (sizeof(Real) == 8) {
+    dtr = La.ck_dt_d;
+    half_dt2 = La.ck_half_dt2_d;
+  } else {
+    dtr = La.ck_dt;
+    half_dt2 = La.ck_half_dt2;
+  }
 
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
     const WorkItem wi = La.work[w];
-    const SolveDesc sd = pick(La, wi.solve);  // by value: no reloads after stores
+    const SolveDesc sd = pick(La, wi.solve);
     const int nc = wi.n_cells;
     __syncthreads();
     load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
     for (int r = 1; r < NL; ++r) {
-      const int sz = nc * F * ipow_c(NP - 2 * r, DIM);
+      const int sz = nc * F * ipow_rt(NP - 2 * r, DIM);
       for (int i = threadIdx.x; i < sz; i += blockDim.x) sm[lay.C[r] + i] = Real(0);
     }
     __syncthreads();
@@ -612,16 +685,16 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
     } else {
       if (active) {
         Real o[F];
-        ck_derivative<DIM, NP, Real, CART>(get_level(sB, NP, 0), sX + cl * F * N,
-                                           sGeo + cl * S::GEO, rho, c_sq, q, o);
+        const Level<Real> L0 = get_level(sB, NP, 0);
+        ck_deriv<DIM, NP, Real, CART>(L0.D, L0.x, sX + cl * F * N, sGeo + cl * S::GEO, rho, c_sq,
+                                      q, o);
 #pragma unroll
         for (int fld = 0; fld < F; ++fld) d1[fld] = -o[fld];
       }
     }
     // Taylor terms 0 and 1; the recursion starts from S = -du/dt
+    Real* sS = sm + lay.Sv;
     Real c0[F];
-    const Real dtr = static_cast<Real>(dt);
-    const Real half_dt2 = static_cast<Real>(0.5 * dt * dt);
     if (active) {
 #pragma unroll
       for (int fld = 0; fld < F; ++fld) {
@@ -630,61 +703,22 @@ __global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
       }
     }
     __syncthreads();
-    double fac = -0.5;
-    double dtp = dt * dt * dt;
-    for (int s = 0; s < n_steps; ++s) {
-      const int r = s / 2;
-      const Level<Real> L = get_level(sB, NP, r);
-      const int m = L.m;
-      const int Nm = ipow_rt(m, DIM);
-      fac /= -(s + 3.0);  // fac = -1/2 prod_{j=2}^{s+2} (-1/(j+1))
-      if (s > 0) dtp *= dt;  // dt^(s+3)
-      const Real fac_t = static_cast<Real>(fac * dtp);
-      Real sn[F];
-      const bool act_l = active && q < Nm;
-      if (act_l)
-        ck_derivative<DIM, NP, Real, CART>(L, sS + cl * F * N, sGeo + cl * S::GEO, rho, c_sq, q, sn);
-      __syncthreads();
-      if (act_l) {
-#pragma unroll
-        for (int fld = 0; fld < F; ++fld) {
-          sS[cl * F * N + fld * Nm + q] = sn[fld];
-          if (r == 0)
-            c0[fld] += fac_t * sn[fld];
-          else
-            sm[lay.C[r] + cl * F * Nm + fld * Nm + q] += fac_t * sn[fld];
-        }
-      }
-      __syncthreads();
-      if (s + 1 < n_steps && (s & 1)) {
-        // L2 projection of S onto the next lower level (degree - 2)
-        const Level<Real> Ln = get_level(sB, NP, r + 1);
-        tensor_all<DIM, Real>(Ln.P, Ln.m, m, sS, F * N, sS, F * N, sT1, sT2, F * N, nc, F);
-      }
-    }
-    // interpolate the lower-level contributions back up and sum
-    const int r_last = (n_steps - 1) / 2;
-    for (int r = r_last; r >= 1; --r) {
-      const Level<Real> Lr = get_level(sB, NP, r);
-      const int m = Lr.m, mp = m + 2;
-      const int Nmp = ipow_rt(mp, DIM);
-      Real* up = (DIM == 2) ? sT2 : sT1;
-      tensor_all<DIM, Real>(Lr.E, mp, m, sm + lay.C[r], F * ipow_rt(m, DIM), up, F * N, sT1, sT2,
-                            F * N, nc, F);
-      if (r - 1 == 0) {
-        if (active) {
-#pragma unroll
-          for (int fld = 0; fld < F; ++fld) c0[fld] += up[cl * F * N + fld * Nmp + q];
-        }
-      } else {
-        for (int idx = threadIdx.x; idx < nc * F * Nmp; idx += blockDim.x) {
-          const int c2 = idx / (F * Nmp);
-          const int rr = idx - c2 * F * Nmp;
-          sm[lay.C[r - 1] + c2 * F * Nmp + rr] += up[c2 * F * N + rr];
-        }
-      }
-      __syncthreads();
-    }
+    CkState<Real> st;
+    st.sB = sB;
+    st.sS = sS;
+    st.sT1 = sm + lay.T1;
+    st.sT2 = sm + lay.T2;
+    st.sm = sm;
+    st.C = lay.C;
+    st.sGeo = sGeo;
+    st.cl = cl;
+    st.q = q;
+    st.nc = nc;
+    st.active = active;
+    st.rho = rho;
+    st.c_sq = c_sq;
+    ck_steps<DIM, NP, Real, CART, 0, NSTEPS>(st, fac, c0);
+    ck_gather<DIM, NP, Real, RLAST>(st, c0);
     if (active) {
       OutT* T = static_cast<OutT*>(sd.Xout);
       const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + q;
