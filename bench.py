@@ -154,6 +154,7 @@ def time_steps(op, dt, steps, warmup, torch, barrier):
     barrier()
     ms = ev0.elapsed_time(ev1)
     launches = op.kernel_launches() - l0
+    op.synchronize()  # raises if a kernel raised its device error flag
     t_end = (warmup + steps) * dt
     errs = op.l2_errors(u, *MODES, t_end)
     return ms, launches, errs, u

@@ -233,8 +233,9 @@ struct CartSmem {
 // an unused branch is if-converted into the executed path).
 //  APPLY       : Aout = k (WaveEquationOperation::apply)
 //  F64_MID/LAST: the reference's RKVectorUpdater arithmetic in FP64
-//  MIX_S1      : first LSRK stage, FP64 state in, FP32 stage input and
-//                float-float accumulator out
+//  MIX_S1      : first LSRK stage, FP64 state in (split into float pairs
+//                in shared memory), FP32 stage input and float-float
+//                accumulator out
 //  MIX_MID     : float-float accumulator in and out, FP32 stage input out
 //  MIX_LAST    : float-float accumulator in, FP64 state out
 //  MIX_UPD     : FP64 in, FP64 out (ADER update u + k)
@@ -296,14 +297,8 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     an = x + sd.f2 * k;
   } else if constexpr (EPI == EPI_F64_LAST) {
     an = a + sd.f1 * k;
-  } else if constexpr (EPI == EPI_MIX_S1) {
-    const float ah = f64_to_f32(a);
-    const float al = f64_to_f32(a - f32_to_f64(ah));
-    xn = static_cast<OutT>(fmaf(sd.f1f, k, ah));
-    float rh, rl;
-    ff_add(ah, al, fmaf(sd.fb_hi, k, sd.fb_lo * k), rh, rl);
-    an = ff_pack(rh, rl);
-  } else if constexpr (EPI == EPI_MIX_MID) {
+  } else if constexpr (EPI == EPI_MIX_MID || EPI == EPI_MIX_S1) {
+    // MIX_S1: the staged FP64 state was split into (hi, lo) in place
     const float ah = ff_hi(a), al = ff_lo(a);
     xn = static_cast<OutT>(fmaf(sd.f1f, k, ah));
     float rh, rl;
@@ -339,6 +334,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   constexpr int F = DIM + 1;
   constexpr int NL = ipow_c(NP, DIM - 1);
   constexpr int H = NP / 2;
+  constexpr bool CONV = sizeof(Real) == 4 && sizeof(InT) == 8;
   const LaunchArgs& La = ca.la;
   const int CB = La.cells_per_block;
   extern __shared__ __align__(128) unsigned char smem_cart[];
@@ -482,12 +478,36 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
       }
     }
     __syncthreads();
+    if constexpr (CONV) {
+      // FP32 operator on FP64 values: each staged value is converted once,
+      // in place, to a float pair (hi in the low word is the operator input).
+      // MIX_S1 splits the accumulator exactly, hi + lo, and continues from
+      // the pair like the middle stages.
+      const int tot = nc * F * N;
+      if constexpr (EPI == EPI_MIX_S1) {
+        for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+          float hi, lo;
+          f64_split(sA[i], hi, lo);
+          sA[i] = ff_pack(hi, lo);
+        }
+      }
+      if (stage_x) {
+        double* sX64 = reinterpret_cast<double*>(sX);
+        for (int i = threadIdx.x; i < tot; i += blockDim.x) sX64[i] = ff_pack(f64_to_f32(sX64[i]), 0.f);
+      }
+      // these generic writes precede the bulk copy that refills the buffer
+      fence_proxy_async();
+      __syncthreads();
+    }
 
     // ---------------------------------------------------------- line phase
     // stage input values as Real, from the X buffer or (X == A) the A buffer
     auto xval = [&](int idx) -> Real {
       if constexpr (sizeof(InT) == 4) {
         return sX[idx];
+      } else if constexpr (CONV) {
+        return reinterpret_cast<const float*>(stage_x ? static_cast<const void*>(sX)
+                                                      : static_cast<const void*>(sA))[2 * idx];
       } else {
         const double* src = stage_x ? reinterpret_cast<const double*>(sX) : sA;
         return to_real<Real>(src[idx]);

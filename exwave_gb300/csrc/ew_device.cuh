@@ -175,6 +175,27 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// a = hi + lo with hi = f64_to_f32(a) and lo the nearest float to the exact
+// remainder a - hi, on the integer pipes: the remainder is the part of the
+// 53-bit significand below hi's 24 bits (at most 2^28 units of a's ulp, one
+// int-to-float conversion), rescaled through its exponent field.  lo is
+// flushed to zero where it would be subnormal (|lo| < 2^-126).
+__device__ __forceinline__ void f64_split(double a, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const unsigned long long mag = b & 0x7fffffffffffffffull;
+  const unsigned long long r = mag + (1ull << 28);
+  const int e = (int)(r >> 52) - 896;
+  const unsigned int m = (unsigned int)(r >> 29) & 0x7fffffu;
+  const bool finite = e > 0 && e < 255;
+  hi = __uint_as_float(e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | ((unsigned int)e << 23) | m)));
+  const long long rem = (long long)(mag - (r & ~((1ull << 29) - 1)));
+  const unsigned int fb = __float_as_uint(__int2float_rn((int)rem));
+  const int ef = (int)((fb >> 23) & 0xffu) + (int)(mag >> 52) - 1075;
+  lo = __uint_as_float((finite && rem != 0 && ef > 0) ? (((fb & 0x807fffffu) | ((unsigned int)ef << 23)) ^ sign)
+                                                      : sign);
+}
+
 template <typename T>
 __device__ __forceinline__ T load_nc(const T* p) {
   return __ldg(p);
