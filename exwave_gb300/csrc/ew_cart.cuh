@@ -13,10 +13,12 @@
 //
 // Input staging: each work item's contiguous block of cells (stage input X
 // and accumulator A) is copied into shared memory with one 1-D bulk copy
-// (cp.async.bulk, TMA engine) per array, completed on an mbarrier; the
-// copies of the next work item are issued before the current one is
-// processed (double buffering).  Waits are bounded; on time-out the kernel
-// raises ERR_WAIT_TIMEOUT and skips the item.
+// (cp.async.bulk, TMA engine) per array, completed on an mbarrier.  The
+// copy of the next item's X is issued before the current one is processed
+// (double buffering); A, read only by the epilogue, has a single buffer
+// refilled at the start of each item, which keeps the block small enough
+// for four resident blocks per SM.  Waits are bounded; on time-out the
+// kernel raises ERR_WAIT_TIMEOUT and stops.
 #pragma once
 
 #include <cstring>
@@ -213,13 +215,19 @@ struct CartSmem {
   static constexpr int F = DIM + 1;
   size_t bar, X, A, Kp, cell, nb, end;
   int xbytes, abytes;  // per buffer
+  // The stage input X is double buffered (the next item's copy is in
+  // flight while the current one is processed).  The accumulator A is only
+  // read by the epilogue: when X is staged on its own, A has one buffer,
+  // refilled at the start of every item; when X == A (first stage), A is
+  // the operator input and is double buffered like X.
+  __host__ __device__ static bool a_single(bool stage_x, bool stage_a) { return stage_a && stage_x; }
   __host__ __device__ CartSmem(int CB, bool stage_x, bool stage_a) {
-    bar = 0;  // 4 mbarriers (X and A, double buffered)
+    bar = 0;  // mbarriers: X / A double buffered (0, 1), single A (2)
     X = 64;
     xbytes = stage_x ? CB * F * N * (int)sizeof(InT) : 0;
     A = X + 2 * (size_t)((xbytes + 127) & ~127);
     abytes = stage_a ? CB * F * N * (int)sizeof(double) : 0;
-    Kp = A + 2 * (size_t)((abytes + 127) & ~127);
+    Kp = A + (a_single(stage_x, stage_a) ? 1 : 2) * (size_t)((abytes + 127) & ~127);
     cell = Kp + (size_t)DIM * CB * N * sizeof(Real);
     // per thread: the neighbours' lines of u_e and p on both sides
     nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
@@ -327,7 +335,8 @@ struct CartArgs {
 };
 
 template <int DIM, int NP, typename Real, typename InT, int EPI>
-__global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
+__global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) == 8) ? 80 : 72))
+    stage_cart_kernel(const CartArgs ca) {
   using OutT = std::conditional_t<sizeof(Real) == 8, double, float>;
   constexpr bool stage_a = EpiTraits<EPI>::stage_a;
   constexpr int N = ipow_c(NP, DIM);
@@ -351,9 +360,10 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   const CartBasis<Real>& B = CartConst<Real>::get();
   const bool stage_x = (sizeof(InT) == 4) || ca.stage_x != 0;
 
-  // issue the copies of work item w into buffer b
-  auto issue = [&](int w, int b) {
-    const WorkItem wi = La.work[w];
+  const bool a_single = CartSmem<DIM, NP, Real, InT>::a_single(stage_x, stage_a);
+  // issue the copies of work item w into buffer b (X, and A unless it has
+  // its own single buffer)
+  auto issue = [&](const WorkItem& wi, int b) {
     const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
     const void* Xg = sdp->X;
     const double* Ag = sdp->A;
@@ -362,10 +372,17 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
     const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
     uint32_t tx = 0;
     if (stage_x) tx += nx;
-    if constexpr (stage_a) tx += na;
+    if (stage_a && !a_single) tx += na;
     mbar_expect_tx(&bars[b], tx);
     if (stage_x) bulk_g2s(smem_cart + lay.X + b * xstride, static_cast<const InT*>(Xg) + c0, nx, &bars[b]);
-    if constexpr (stage_a) bulk_g2s(smem_cart + lay.A + b * astride, Ag + c0, na, &bars[b]);
+    if (stage_a && !a_single) bulk_g2s(smem_cart + lay.A + b * astride, Ag + c0, na, &bars[b]);
+  };
+  // the single A buffer of work item w
+  auto issue_a = [&](const WorkItem& wi) {
+    const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
+    const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
+    mbar_expect_tx(&bars[2], na);
+    bulk_g2s(smem_cart + lay.A, sdp->A + (size_t)wi.cell_begin * F * N, na, &bars[2]);
   };
 
   // line task of this thread: (cell, direction, line), the same for every item
@@ -381,35 +398,29 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
   InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
   const int nstride = blockDim.x;
-  // Neighbour lines (u_e and p, both sides) of item w that are not in the
+  // Neighbour lines (u_e and p, both sides) of item wi that are not in the
   // item's own block: asynchronous copies from L2 into this thread's slot.
-  auto prefetch_nb = [&](int w, int* nbs) {
+  auto prefetch_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
     nbs[0] = nbs[1] = -EW_BC_HARD_WALL_ID;
-    if (w < La.n_work) {
-      const WorkItem wi = La.work[w];
-      const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
-      const int32_t* nbr = sdp->nbr;
-      const int64_t ncells = sdp->n_cells;
-      const InT* Xg = static_cast<const InT*>(sdp->X);
-      if (tcl < wi.n_cells) {
-        const int cell = wi.cell_begin + tcl;
+    const InT* Xg = static_cast<const InT*>(sd.X);
+    if (tcl < wi.n_cells) {
+      const int cell = wi.cell_begin + tcl;
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          int nb = nbr[(size_t)cell * 2 * DIM + 2 * te + s];
-          if (nb >= ncells) {
-            atomicOr(La.err, ERR_BAD_NEIGHBOR);
-            nb = cell;
-          }
-          nbs[s] = nb;
-          const int nl = nb - wi.cell_begin;
-          if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
-            const InT* xn = Xg + (size_t)nb * F * N;
+      for (int s = 0; s < 2; ++s) {
+        int nb = sd.nbr[(size_t)cell * 2 * DIM + 2 * te + s];
+        if (nb >= sd.n_cells) {
+          atomicOr(La.err, ERR_BAD_NEIGHBOR);
+          nb = cell;
+        }
+        nbs[s] = nb;
+        const int nl = nb - wi.cell_begin;
+        if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
+          const InT* xn = Xg + (size_t)nb * F * N;
 #pragma unroll
-            for (int j = 0; j < NP; ++j) {
-              cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, xn + te * N + tbase + j * tstr);
-              cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride,
-                                    xn + DIM * N + tbase + j * tstr);
-            }
+          for (int j = 0; j < NP; ++j) {
+            cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, xn + te * N + tbase + j * tstr);
+            cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride,
+                                  xn + DIM * N + tbase + j * tstr);
           }
         }
       }
@@ -420,23 +431,38 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
     fence_barrier_init();
   }
   __syncthreads();
-  if (ca.tma && threadIdx.x == 0 && (int)blockIdx.x < La.n_work) issue(blockIdx.x, 0);
+  if (ca.tma && threadIdx.x == 0 && (int)blockIdx.x < La.n_work) issue(La.work[blockIdx.x], 0);
   int nbs[2];
 
   uint32_t phase = 0;  // bit b: parity of the next wait on buffer b
   int it = 0;
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
     const int b = it & 1;
+    const bool has_next = w + (int)gridDim.x < La.n_work;
     const WorkItem wi = La.work[w];
     // by value: the fields live in registers instead of being re-read after
     // every store (a reference could alias the output arrays)
     const SolveDesc sd = La.solves ? La.solves[wi.solve] : La.single;
     const int nc = wi.n_cells;
     InT* sX = reinterpret_cast<InT*>(smem_cart + lay.X + b * xstride);
-    double* sA = reinterpret_cast<double*>(smem_cart + lay.A + b * astride);
+    double* sA = reinterpret_cast<double*>(smem_cart + lay.A + (a_single ? 0 : b * astride));
+    // the single A buffer was last read before the previous end-of-item
+    // barrier: refill it now, it is needed only by the epilogue
+    if (ca.tma && a_single && threadIdx.x == 0) {
+      fence_proxy_async();
+      issue_a(wi);
+    }
+    bool a_ok = true, a_ready = !(ca.tma && a_single);
+    auto wait_a = [&]() {
+      if (!a_ready) {
+        a_ok = mbar_wait(&bars[2], (uint32_t)it & 1u);
+        a_ready = true;
+      }
+    };
     // per-cell constants (prepared on the host, see ew_create)
     {
       const Real* gc = static_cast<const Real*>(sd.cellc) + (size_t)wi.cell_begin * kCellConsts;
@@ -445,14 +471,13 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
     const bool tactive = tcl < nc;
     // this item's non-local neighbour lines: in flight during the bulk-copy
     // wait and the own-line contractions, awaited just before the fluxes
-    prefetch_nb(w, nbs);
+    prefetch_nb(wi, sd, nbs);
     if (ca.tma) {
       // prefetch the next item into the other buffer (its previous contents
       // were consumed before the end-of-item barrier of the last iteration)
-      const bool has_next = w + (int)gridDim.x < La.n_work;
       if (threadIdx.x == 0 && has_next) {
         fence_proxy_async();
-        issue(w + gridDim.x, b ^ 1);
+        issue(La.work[w + gridDim.x], b ^ 1);
       }
       const bool ok = mbar_wait(&bars[b], (phase >> b) & 1u);
       phase ^= (1u << b);
@@ -462,6 +487,7 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
         if (threadIdx.x == 0) {
           atomicOr(La.err, ERR_WAIT_TIMEOUT);
           if (has_next) mbar_wait(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+          if (a_single) mbar_wait(&bars[2], (uint32_t)it & 1u);
         }
         cp_async_wait_all();
         break;
@@ -626,7 +652,8 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
         // finish u_e on this line (x-lines are contiguous: paired stores)
         const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + e * N + base;
         const int l0 = xo + e * N + base;
-        {
+        wait_a();
+        if (a_ok) {
           const bool paired = NP % 2 == 0 && e == 0 &&
                               (reinterpret_cast<uintptr_t>(sd.Aout) & 15) == 0 &&
                               (reinterpret_cast<uintptr_t>(sd.Xout) & 7) == 0;
@@ -658,7 +685,8 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
     Real src_val = Real(0);
     if (src_local >= 0 && src_local < nc)
       src_val = static_cast<Real>(sd.src_amp * ricker(*sd.time + sd.c_stage * sd.dt, sd.src_f0, sd.src_t0));
-    for (int idx = threadIdx.x; idx < nc * N; idx += blockDim.x) {
+    wait_a();
+    for (int idx = threadIdx.x; a_ok && idx < nc * N; idx += blockDim.x) {
       const int cl = idx / N;
       const int q = idx - cl * N;
       Real k = sKp[cl * N + q];
@@ -673,7 +701,16 @@ __global__ void __launch_bounds__(256, 3) stage_cart_kernel(const CartArgs ca) {
       if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
       sd.Aout[g] = an;
     }
-    __syncthreads();
+    if (__syncthreads_or(!a_ok)) {
+      // the accumulator copy timed out: stop as on an X time-out
+      if (threadIdx.x == 0) {
+        atomicOr(La.err, ERR_WAIT_TIMEOUT);
+        if (has_next) mbar_wait(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+        mbar_wait(&bars[2], (uint32_t)it & 1u);
+      }
+      cp_async_wait_all();
+      break;
+    }
   }
 }
 
