@@ -505,7 +505,7 @@ void split(double v, float* hi, float* lo) {
 
 bool cart_variant_in32(int cv) {
   return cv == ew::CV_MIX_APPLY32 || cv == ew::CV_MIX_MID || cv == ew::CV_MIX_LAST ||
-         cv == ew::CV_MIX_UPD;
+         cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF;
 }
 bool cart_variant_apply(int cv) {
   return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32;
@@ -857,6 +857,59 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
     rc = launch_stage(ctx, STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1],
                       xout[s - 1], vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
     if (rc) return rc;
+  }
+  return EW_OK;
+}
+
+int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np || n_steps < 0)
+    return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_steps: invalid vectors or step count");
+  if (n_steps == 0)
+    return cudaMemcpyAsync(vec_np, vec_n, (size_t)ctx->n_dofs * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream) == cudaSuccess
+               ? EW_OK
+               : fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
+  using namespace ew;
+  if (!ctx->mixed || !ctx->cart) {
+    // one step at a time; the state alternates between the two vectors
+    double* a = vec_n;
+    double* b = vec_np;
+    for (int64_t s = 0; s < n_steps; ++s) {
+      if ((rc = ew_lsrk45_step(ctx, dt, a, b))) return rc;
+      std::swap(a, b);
+    }
+    if (a != vec_np &&
+        cudaMemcpyAsync(vec_np, a, (size_t)ctx->n_dofs * sizeof(double), cudaMemcpyDeviceToDevice,
+                        ctx->stream) != cudaSuccess)
+      return fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
+    return EW_OK;
+  }
+  // Mixed, Cartesian.  The accumulator lives in vec_np; between the steps
+  // the state is a float pair in vec_n (written by the last stage, read by
+  // the next first stage, which no longer needs the previous state once it
+  // has run); the final step leaves FP64 in vec_np.
+  const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
+  const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
+                        0.0};
+  float* X0 = ctx->d_x32[0];
+  float* X1 = ctx->d_x32[1];
+  const float* xin[4] = {X0, X1, X0, X1};
+  float* xout[4] = {X1, X0, X1, nullptr};
+  for (int64_t step = 0; step < n_steps; ++step) {
+    const bool last_step = step + 1 == n_steps;
+    rc = launch_stage(ctx, STAGE_MIX_IN64, step == 0 ? CV_MIX_S1 : CV_MIX_S1_FF, vec_n, vec_n, X0,
+                      vec_np, MODE_RK_MID, f1[0], f2[0], 1.0f);
+    if (rc) return rc;
+    for (int s = 1; s < 5; ++s) {
+      const bool last = s == 4;
+      const int cv = !last ? CV_MIX_MID : (last_step ? CV_MIX_LAST : CV_MIX_LAST_FF);
+      double* out = (last && !last_step) ? vec_n : vec_np;
+      rc = launch_stage(ctx, STAGE_MIX_IN32, cv, vec_np, xin[s - 1], xout[s - 1], out,
+                        last ? MODE_RK_LAST : MODE_RK_MID, f1[s], f2[s], 1.0f);
+      if (rc) return rc;
+    }
   }
   return EW_OK;
 }

@@ -208,8 +208,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 // 1/tau, 1/h_e (3), and per face (tau of the neighbour, 1/(tau + tau_nb)).
 constexpr int kCellConsts = 4 + 3 + 6 * 2;
 
-// Shared-memory layout of the Cartesian kernel (bytes).
-template <int DIM, int NP, typename Real, typename InT>
+// Shared-memory layout of the Cartesian kernel (bytes).  SlotT is the
+// element type of the neighbour-line slots.
+template <int DIM, int NP, typename Real, typename InT, typename SlotT = InT>
 struct CartSmem {
   static constexpr int N = ipow_c(NP, DIM);
   static constexpr int F = DIM + 1;
@@ -232,7 +233,7 @@ struct CartSmem {
     // per thread: the neighbours' lines of u_e and p on both sides
     nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
     const int threads = CB * DIM * ipow_c(NP, DIM - 1);
-    end = nb + (size_t)threads * 4 * NP * sizeof(InT);
+    end = nb + (size_t)threads * 4 * NP * sizeof(SlotT);
     end = (end + 127) & ~(size_t)127;
   }
 };
@@ -247,6 +248,10 @@ struct CartSmem {
 //  MIX_MID     : float-float accumulator in and out, FP32 stage input out
 //  MIX_LAST    : float-float accumulator in, FP64 state out
 //  MIX_UPD     : FP64 in, FP64 out (ADER update u + k)
+//  MIX_S1_FF   : first stage of a step inside a multi-step call: the state
+//                is already a float pair (hi, lo) in an 8-byte slot
+//  MIX_LAST_FF : last stage of such a step: the new state stays a float
+//                pair (no rounding to FP64) for the next step's MIX_S1_FF
 // Within an LSRK step the mixed path keeps the accumulator as an unevaluated
 // sum hi + lo of two floats (about 48 significant bits) in the 8-byte slot
 // of the FP64 vector, updated with error-free transformations on the FP32
@@ -258,14 +263,23 @@ enum Epi : int {
   EPI_MIX_S1 = 3,
   EPI_MIX_MID = 4,
   EPI_MIX_LAST = 5,
-  EPI_MIX_UPD = 6
+  EPI_MIX_UPD = 6,
+  EPI_MIX_S1_FF = 7,
+  EPI_MIX_LAST_FF = 8
 };
 
 template <int EPI>
 struct EpiTraits {
   static constexpr bool stage_a = EPI != EPI_APPLY;
-  static constexpr bool writes_x = EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID;
+  static constexpr bool writes_x =
+      EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_S1_FF;
+  // the state arrives as float pairs: the operator reads the hi words, also
+  // of the neighbours' lines (4-byte slots)
+  static constexpr bool pairs_in = EPI == EPI_MIX_S1_FF;
 };
+
+template <typename InT, int EPI>
+using SlotOf = std::conditional_t<EpiTraits<EPI>::pairs_in, float, InT>;
 
 // (hi, lo) + b with hi + lo normalised (Knuth two-sum, fast renormalisation)
 __device__ __forceinline__ void ff_add(float hi, float lo, float b, float& rh, float& rl) {
@@ -305,7 +319,7 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     an = x + sd.f2 * k;
   } else if constexpr (EPI == EPI_F64_LAST) {
     an = a + sd.f1 * k;
-  } else if constexpr (EPI == EPI_MIX_MID || EPI == EPI_MIX_S1) {
+  } else if constexpr (EPI == EPI_MIX_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_S1_FF) {
     // MIX_S1: the staged FP64 state was split into (hi, lo) in place
     const float ah = ff_hi(a), al = ff_lo(a);
     xn = static_cast<OutT>(fmaf(sd.f1f, k, ah));
@@ -316,6 +330,10 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     float rh, rl;
     ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
     an = f32_to_f64(rh) + f32_to_f64(rl);
+  } else if constexpr (EPI == EPI_MIX_LAST_FF) {
+    float rh, rl;
+    ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
+    an = ff_pack(rh, rl);
   } else {  // EPI_MIX_UPD
     an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
   }
@@ -344,10 +362,12 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   constexpr int NL = ipow_c(NP, DIM - 1);
   constexpr int H = NP / 2;
   constexpr bool CONV = sizeof(Real) == 4 && sizeof(InT) == 8;
+  constexpr bool PAIRS = EpiTraits<EPI>::pairs_in;
+  using SlotT = SlotOf<InT, EPI>;
   const LaunchArgs& La = ca.la;
   const int CB = La.cells_per_block;
   extern __shared__ __align__(128) unsigned char smem_cart[];
-  const CartSmem<DIM, NP, Real, InT> lay(CB, ca.stage_x != 0, stage_a);
+  const CartSmem<DIM, NP, Real, InT, SlotT> lay(CB, ca.stage_x != 0, stage_a);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_cart + lay.bar);
   const size_t xstride = (size_t)((lay.xbytes + 127) & ~127);
   const size_t astride = (size_t)((lay.abytes + 127) & ~127);
@@ -360,7 +380,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   const CartBasis<Real>& B = CartConst<Real>::get();
   const bool stage_x = (sizeof(InT) == 4) || ca.stage_x != 0;
 
-  const bool a_single = CartSmem<DIM, NP, Real, InT>::a_single(stage_x, stage_a);
+  const bool a_single = CartSmem<DIM, NP, Real, InT, SlotT>::a_single(stage_x, stage_a);
   // issue the copies of work item w into buffer b (X, and A unless it has
   // its own single buffer)
   auto issue = [&](const WorkItem& wi, int b) {
@@ -396,7 +416,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   }
   const int tstr = dir_stride(te, NP);
   // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
-  InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
+  SlotT* nslot = reinterpret_cast<SlotT*>(smem_cart + lay.nb) + threadIdx.x;
   const int nstride = blockDim.x;
   // Neighbour lines (u_e and p, both sides) of item wi that are not in the
   // item's own block: asynchronous copies from L2 into this thread's slot.
@@ -415,12 +435,19 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
         nbs[s] = nb;
         const int nl = nb - wi.cell_begin;
         if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
-          const InT* xn = Xg + (size_t)nb * F * N;
+          const size_t o = (size_t)nb * F * N;
 #pragma unroll
           for (int j = 0; j < NP; ++j) {
-            cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, xn + te * N + tbase + j * tstr);
-            cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride,
-                                  xn + DIM * N + tbase + j * tstr);
+            const size_t iu = o + te * N + tbase + j * tstr, ip = o + DIM * N + tbase + j * tstr;
+            if constexpr (PAIRS) {
+              // hi word (low address) of each 8-byte pair
+              const float* Xf = static_cast<const float*>(sd.X);
+              cp_async<4>(nslot + ((2 * s) * NP + j) * nstride, Xf + 2 * iu);
+              cp_async<4>(nslot + ((2 * s + 1) * NP + j) * nstride, Xf + 2 * ip);
+            } else {
+              cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, Xg + iu);
+              cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride, Xg + ip);
+            }
           }
         }
       }
@@ -504,7 +531,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
       }
     }
     __syncthreads();
-    if constexpr (CONV) {
+    if constexpr (CONV && !PAIRS) {
       // FP32 operator on FP64 values: each staged value is converted once,
       // in place, to a float pair (hi in the low word is the operator input).
       // MIX_S1 splits the accumulator exactly, hi + lo, and continues from

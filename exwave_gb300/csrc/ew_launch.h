@@ -34,7 +34,9 @@ enum CartVariant : int {
   CV_MIX_MID = 6,     // mixed LSRK stages 2..4
   CV_MIX_LAST = 7,    // mixed LSRK stage 5 (FP64 state out)
   CV_MIX_UPD = 8,     // mixed ADER update u + M^-1 A(T)
-  N_CART_VARIANTS = 9
+  CV_MIX_S1_FF = 9,   // mixed stage 1, state held as float pairs (multi-step calls)
+  CV_MIX_LAST_FF = 10,  // mixed stage 5, state left as float pairs
+  N_CART_VARIANTS = 11
 };
 
 // Launcher of the Cartesian line kernel.

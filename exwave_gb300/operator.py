@@ -104,6 +104,10 @@ class WaveEquationOperation:
     def lsrk45_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_lsrk45_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 
+    def lsrk45_steps(self, dt, n_steps, vec_n, vec_np):
+        """n_steps LSRK45 steps in one call (vec_n in, clobbered; vec_np out)."""
+        self._chk(self.L.ew_lsrk45_steps(self.ctx, dt, int(n_steps), _ptr(vec_n), _ptr(vec_np)))
+
     def ader_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_ader_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 

@@ -116,6 +116,16 @@ int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const doubl
  * the reference. */
 int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
 
+/* n_steps LSRK45 steps in one call: the reference's time loop
+ * (explicit_wave.cc:779-799) calling perform_time_step and swapping the two
+ * vectors n_steps times.  On entry vec_n holds u^n; on return vec_np holds
+ * u^{n+n_steps} and vec_n is undefined.  With mixed precision on Cartesian
+ * meshes the state between two steps of the call is kept as an unevaluated
+ * float pair (hi + lo, about 48 significant bits) instead of being rounded
+ * to FP64, so the first stage of each following step reads it pre-split;
+ * the final state is FP64. */
+int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, double* vec_np);
+
 /* The same LSRK45 step as ew_lsrk45_step, for callers that cannot have the
  * library allocate device memory: it has no counterpart in the reference.
  * Code that runs the step inside an application which owns all device

@@ -97,6 +97,47 @@ def test_lsrk45_steps(env, case):
     assert err < FP64_TOL, err
 
 
+@pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 3, 8, 11)], ids=ids)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("n_steps", [1, 2, 5])
+def test_lsrk45_steps_call(env, case, precision, n_steps):
+    """ew_lsrk45_steps against n_steps calls of ew_lsrk45_step and the FP64
+    oracle.  FP64: identical.  Mixed: on Cartesian meshes the call keeps the
+    state as a float pair between its steps (exactly the FP64 state the
+    single-step path would round to) and runs other kernel instantiations,
+    whose FP32 operations may round differently; the two paths then agree to
+    FP32 round-off (1e-6 relative after 5 steps) and stay as close to the
+    FP64 oracle as the single-step path."""
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=3)
+    op = ew.WaveEquationOperation(m, k, precision=precision)
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    u0h = o.project_reference(2)
+    u0 = torch.from_numpy(u0h.copy()).cuda()
+    dt = o.time_step(0.3 / k ** 1.5)
+    vn, vnp = u0.clone(), torch.zeros_like(u0)
+    for _ in range(n_steps):
+        op.lsrk45_step(dt, vn, vnp)
+        vn, vnp = vnp, vn
+    a, b = u0.clone(), torch.full_like(u0, float("nan"))
+    op.lsrk45_steps(dt, n_steps, a, b)
+    op.synchronize()
+    single, multi = vn.cpu().numpy(), b.cpu().numpy()
+    scale = np.abs(single).max()
+    if precision == "fp64":
+        assert np.array_equal(multi, single)
+        return
+    assert np.abs(multi - single).max() / scale < 1e-6
+    x, y = u0h.copy(), np.zeros_like(u0h)
+    for _ in range(n_steps):
+        o.lsrk45_step(dt, x, y)
+        x, y = y, x
+    e_single = np.abs(single - x).max() / scale
+    e_multi = np.abs(multi - x).max() / scale
+    assert e_multi < 1e-5 and e_multi < 2.0 * e_single + 1e-9, (e_multi, e_single)
+
+
 @pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 5, 9, 10, 13)], ids=ids)
 @pytest.mark.parametrize("post", [False, True])
 def test_ader_step(env, case, post):
