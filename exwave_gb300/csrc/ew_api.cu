@@ -505,7 +505,7 @@ void split(double v, float* hi, float* lo) {
 
 bool cart_variant_in32(int cv) {
   return cv == ew::CV_MIX_APPLY32 || cv == ew::CV_MIX_MID || cv == ew::CV_MIX_LAST ||
-         cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF;
+         cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF || cv == ew::CV_MIX_S1_FF;
 }
 bool cart_variant_apply(int cv) {
   return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32;
@@ -533,10 +533,11 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
     // line kernel: stage X unless it is the accumulator itself (first LSRK
     // stage); bulk copies need 16-byte alignment
     const size_t in_sz = cart_variant_in32(cvar) ? 4 : 8;
+    const size_t a_sz = cvar == ew::CV_MIX_S1_FF ? 4 : 8;  // lo array of a float-pair state
     const bool sa = !cart_variant_apply(cvar);
     const int sx = (sa && static_cast<const void*>(A) == X && in_sz == 8) ? 0 : 1;
     const size_t cell_elems = (size_t)c->F * c->N;
-    const bool tma = (cell_elems * in_sz) % 16 == 0 && (cell_elems * 8) % 16 == 0 &&
+    const bool tma = (cell_elems * in_sz) % 16 == 0 && (cell_elems * a_sz) % 16 == 0 &&
                      (reinterpret_cast<uintptr_t>(X) % 16) == 0 &&
                      (!sa || (reinterpret_cast<uintptr_t>(A) % 16) == 0);
     a.work = c->d_work_cart;
@@ -886,28 +887,44 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
       return fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
     return EW_OK;
   }
-  // Mixed, Cartesian.  The accumulator lives in vec_np; between the steps
-  // the state is a float pair in vec_n (written by the last stage, read by
-  // the next first stage, which no longer needs the previous state once it
-  // has run); the final step leaves FP64 in vec_np.
+  // Mixed, Cartesian.  The accumulator lives in vec_np.  Between two steps
+  // the state is a float pair held as two FP32 arrays: hi in the stage
+  // input buffer the last stage does not read, lo in vec_n's memory (free
+  // once the call's first stage has read the FP64 input).  The next first
+  // stage reads hi like a middle stage reads its input; the call's final
+  // step writes FP64 to vec_np.
   const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
   const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
                         0.0};
-  float* X0 = ctx->d_x32[0];
-  float* X1 = ctx->d_x32[1];
-  const float* xin[4] = {X0, X1, X0, X1};
-  float* xout[4] = {X1, X0, X1, nullptr};
+  float* xb[2] = {ctx->d_x32[0], ctx->d_x32[1]};
+  float* lo = reinterpret_cast<float*>(vec_n);
+  int hi = -1;  // stage-input buffer holding the state's hi part
   for (int64_t step = 0; step < n_steps; ++step) {
     const bool last_step = step + 1 == n_steps;
-    rc = launch_stage(ctx, STAGE_MIX_IN64, step == 0 ? CV_MIX_S1 : CV_MIX_S1_FF, vec_n, vec_n, X0,
-                      vec_np, MODE_RK_MID, f1[0], f2[0], 1.0f);
+    int cur;  // buffer of the next stage input
+    if (step == 0) {
+      cur = 0;
+      rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, xb[cur], vec_np, MODE_RK_MID,
+                        f1[0], f2[0], 1.0f);
+    } else {
+      cur = hi ^ 1;
+      rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_S1_FF, reinterpret_cast<const double*>(lo), xb[hi],
+                        xb[cur], vec_np, MODE_RK_MID, f1[0], f2[0], 1.0f);
+    }
     if (rc) return rc;
     for (int s = 1; s < 5; ++s) {
-      const bool last = s == 4;
-      const int cv = !last ? CV_MIX_MID : (last_step ? CV_MIX_LAST : CV_MIX_LAST_FF);
-      double* out = (last && !last_step) ? vec_n : vec_np;
-      rc = launch_stage(ctx, STAGE_MIX_IN32, cv, vec_np, xin[s - 1], xout[s - 1], out,
-                        last ? MODE_RK_LAST : MODE_RK_MID, f1[s], f2[s], 1.0f);
+      if (s < 4) {
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, vec_np, xb[cur], xb[cur ^ 1], vec_np,
+                          MODE_RK_MID, f1[s], f2[s], 1.0f);
+        cur ^= 1;
+      } else if (last_step) {
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_LAST, vec_np, xb[cur], nullptr, vec_np,
+                          MODE_RK_LAST, f1[s], f2[s], 1.0f);
+      } else {
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_LAST_FF, vec_np, xb[cur], xb[cur ^ 1],
+                          reinterpret_cast<double*>(lo), MODE_RK_LAST, f1[s], f2[s], 1.0f);
+        hi = cur ^ 1;
+      }
       if (rc) return rc;
     }
   }

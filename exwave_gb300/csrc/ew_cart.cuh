@@ -208,9 +208,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 // 1/tau, 1/h_e (3), and per face (tau of the neighbour, 1/(tau + tau_nb)).
 constexpr int kCellConsts = 4 + 3 + 6 * 2;
 
-// Shared-memory layout of the Cartesian kernel (bytes).  SlotT is the
-// element type of the neighbour-line slots.
-template <int DIM, int NP, typename Real, typename InT, typename SlotT = InT>
+// Shared-memory layout of the Cartesian kernel (bytes); AB is the size of
+// one staged accumulator element (8: FP64 or float pair, 4: the lo part).
+template <int DIM, int NP, typename Real, typename InT, int AB = 8>
 struct CartSmem {
   static constexpr int N = ipow_c(NP, DIM);
   static constexpr int F = DIM + 1;
@@ -227,13 +227,13 @@ struct CartSmem {
     X = 64;
     xbytes = stage_x ? CB * F * N * (int)sizeof(InT) : 0;
     A = X + 2 * (size_t)((xbytes + 127) & ~127);
-    abytes = stage_a ? CB * F * N * (int)sizeof(double) : 0;
+    abytes = stage_a ? CB * F * N * AB : 0;
     Kp = A + (a_single(stage_x, stage_a) ? 1 : 2) * (size_t)((abytes + 127) & ~127);
     cell = Kp + (size_t)DIM * CB * N * sizeof(Real);
     // per thread: the neighbours' lines of u_e and p on both sides
     nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
     const int threads = CB * DIM * ipow_c(NP, DIM - 1);
-    end = nb + (size_t)threads * 4 * NP * sizeof(SlotT);
+    end = nb + (size_t)threads * 4 * NP * sizeof(InT);
     end = (end + 127) & ~(size_t)127;
   }
 };
@@ -249,9 +249,11 @@ struct CartSmem {
 //  MIX_LAST    : float-float accumulator in, FP64 state out
 //  MIX_UPD     : FP64 in, FP64 out (ADER update u + k)
 //  MIX_S1_FF   : first stage of a step inside a multi-step call: the state
-//                is already a float pair (hi, lo) in an 8-byte slot
-//  MIX_LAST_FF : last stage of such a step: the new state stays a float
-//                pair (no rounding to FP64) for the next step's MIX_S1_FF
+//                is a float pair held as two FP32 arrays, hi (the stage
+//                input X, read like a middle stage's) and lo (staged in
+//                place of A)
+//  MIX_LAST_FF : last stage of such a step: the new state is left as that
+//                pair, hi to Xout and lo to Aout (no rounding to FP64)
 // Within an LSRK step the mixed path keeps the accumulator as an unevaluated
 // sum hi + lo of two floats (about 48 significant bits) in the 8-byte slot
 // of the FP64 vector, updated with error-free transformations on the FP32
@@ -271,15 +273,14 @@ enum Epi : int {
 template <int EPI>
 struct EpiTraits {
   static constexpr bool stage_a = EPI != EPI_APPLY;
-  static constexpr bool writes_x =
-      EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_S1_FF;
-  // the state arrives as float pairs: the operator reads the hi words, also
-  // of the neighbours' lines (4-byte slots)
-  static constexpr bool pairs_in = EPI == EPI_MIX_S1_FF;
+  static constexpr bool writes_x = EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID ||
+                                   EPI == EPI_MIX_S1_FF || EPI == EPI_MIX_LAST_FF;
+  // A is the FP32 lo array of a float-pair state whose hi array is X
+  static constexpr bool lo_in = EPI == EPI_MIX_S1_FF;
+  // the new state is written as hi (Xout) and lo (Aout, FP32) arrays
+  static constexpr bool lo_out = EPI == EPI_MIX_LAST_FF;
+  static constexpr int a_elem = lo_in ? 4 : 8;
 };
-
-template <typename InT, int EPI>
-using SlotOf = std::conditional_t<EpiTraits<EPI>::pairs_in, float, InT>;
 
 // (hi, lo) + b with hi + lo normalised (Knuth two-sum, fast renormalisation)
 __device__ __forceinline__ void ff_add(float hi, float lo, float b, float& rh, float& rl) {
@@ -333,6 +334,7 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
   } else if constexpr (EPI == EPI_MIX_LAST_FF) {
     float rh, rl;
     ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
+    xn = static_cast<OutT>(rh);
     an = ff_pack(rh, rl);
   } else {  // EPI_MIX_UPD
     an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
@@ -362,12 +364,13 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   constexpr int NL = ipow_c(NP, DIM - 1);
   constexpr int H = NP / 2;
   constexpr bool CONV = sizeof(Real) == 4 && sizeof(InT) == 8;
-  constexpr bool PAIRS = EpiTraits<EPI>::pairs_in;
-  using SlotT = SlotOf<InT, EPI>;
+  constexpr bool LO_IN = EpiTraits<EPI>::lo_in;
+  constexpr bool LO_OUT = EpiTraits<EPI>::lo_out;
+  constexpr int A_ELEM = EpiTraits<EPI>::a_elem;
   const LaunchArgs& La = ca.la;
   const int CB = La.cells_per_block;
   extern __shared__ __align__(128) unsigned char smem_cart[];
-  const CartSmem<DIM, NP, Real, InT, SlotT> lay(CB, ca.stage_x != 0, stage_a);
+  const CartSmem<DIM, NP, Real, InT, A_ELEM> lay(CB, ca.stage_x != 0, stage_a);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_cart + lay.bar);
   const size_t xstride = (size_t)((lay.xbytes + 127) & ~127);
   const size_t astride = (size_t)((lay.abytes + 127) & ~127);
@@ -380,29 +383,30 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   const CartBasis<Real>& B = CartConst<Real>::get();
   const bool stage_x = (sizeof(InT) == 4) || ca.stage_x != 0;
 
-  const bool a_single = CartSmem<DIM, NP, Real, InT, SlotT>::a_single(stage_x, stage_a);
+  const bool a_single = CartSmem<DIM, NP, Real, InT, A_ELEM>::a_single(stage_x, stage_a);
   // issue the copies of work item w into buffer b (X, and A unless it has
   // its own single buffer)
   auto issue = [&](const WorkItem& wi, int b) {
     const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
     const void* Xg = sdp->X;
-    const double* Ag = sdp->A;
     const size_t c0 = (size_t)wi.cell_begin * F * N;
+    const char* Ag = reinterpret_cast<const char*>(sdp->A) + c0 * A_ELEM;
     const uint32_t nx = (uint32_t)(wi.n_cells * F * N * sizeof(InT));
-    const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
+    const uint32_t na = (uint32_t)(wi.n_cells * F * N * A_ELEM);
     uint32_t tx = 0;
     if (stage_x) tx += nx;
     if (stage_a && !a_single) tx += na;
     mbar_expect_tx(&bars[b], tx);
     if (stage_x) bulk_g2s(smem_cart + lay.X + b * xstride, static_cast<const InT*>(Xg) + c0, nx, &bars[b]);
-    if (stage_a && !a_single) bulk_g2s(smem_cart + lay.A + b * astride, Ag + c0, na, &bars[b]);
+    if (stage_a && !a_single) bulk_g2s(smem_cart + lay.A + b * astride, Ag, na, &bars[b]);
   };
   // the single A buffer of work item w
   auto issue_a = [&](const WorkItem& wi) {
     const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
-    const uint32_t na = (uint32_t)(wi.n_cells * F * N * sizeof(double));
+    const uint32_t na = (uint32_t)(wi.n_cells * F * N * A_ELEM);
     mbar_expect_tx(&bars[2], na);
-    bulk_g2s(smem_cart + lay.A, sdp->A + (size_t)wi.cell_begin * F * N, na, &bars[2]);
+    bulk_g2s(smem_cart + lay.A, reinterpret_cast<const char*>(sdp->A) + (size_t)wi.cell_begin * F * N * A_ELEM,
+             na, &bars[2]);
   };
 
   // line task of this thread: (cell, direction, line), the same for every item
@@ -416,7 +420,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   }
   const int tstr = dir_stride(te, NP);
   // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
-  SlotT* nslot = reinterpret_cast<SlotT*>(smem_cart + lay.nb) + threadIdx.x;
+  InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
   const int nstride = blockDim.x;
   // Neighbour lines (u_e and p, both sides) of item wi that are not in the
   // item's own block: asynchronous copies from L2 into this thread's slot.
@@ -439,15 +443,8 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
 #pragma unroll
           for (int j = 0; j < NP; ++j) {
             const size_t iu = o + te * N + tbase + j * tstr, ip = o + DIM * N + tbase + j * tstr;
-            if constexpr (PAIRS) {
-              // hi word (low address) of each 8-byte pair
-              const float* Xf = static_cast<const float*>(sd.X);
-              cp_async<4>(nslot + ((2 * s) * NP + j) * nstride, Xf + 2 * iu);
-              cp_async<4>(nslot + ((2 * s + 1) * NP + j) * nstride, Xf + 2 * ip);
-            } else {
-              cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, Xg + iu);
-              cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride, Xg + ip);
-            }
+            cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, Xg + iu);
+            cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride, Xg + ip);
           }
         }
       }
@@ -477,12 +474,31 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
     const int nc = wi.n_cells;
     InT* sX = reinterpret_cast<InT*>(smem_cart + lay.X + b * xstride);
     double* sA = reinterpret_cast<double*>(smem_cart + lay.A + (a_single ? 0 : b * astride));
+    // accumulator value of a staged point: FP64 / float pair, or the pair
+    // assembled from the hi (X) and lo arrays
+    auto aval = [&](int idx) -> double {
+      if constexpr (!stage_a) {
+        return 0.0;
+      } else if constexpr (LO_IN) {
+        return ff_pack(static_cast<float>(sX[idx]), reinterpret_cast<const float*>(sA)[idx]);
+      } else {
+        return sA[idx];
+      }
+    };
     // the single A buffer was last read before the previous end-of-item
     // barrier: refill it now, it is needed only by the epilogue
     if (ca.tma && a_single && threadIdx.x == 0) {
       fence_proxy_async();
       issue_a(wi);
     }
+    // one value's outputs: next stage input and accumulator / new state
+    auto store_out = [&](size_t g, OutT xn, double an) {
+      if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
+      if constexpr (LO_OUT)
+        reinterpret_cast<float*>(sd.Aout)[g] = ff_lo(an);
+      else
+        sd.Aout[g] = an;
+    };
     bool a_ok = true, a_ready = !(ca.tma && a_single);
     auto wait_a = [&]() {
       if (!a_ready) {
@@ -525,13 +541,16 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
         const InT* gx = static_cast<const InT*>(sd.X) + c0;
         for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sX[i] = gx[i];
       }
-      if constexpr (stage_a) {
+      if constexpr (stage_a && LO_IN) {
+        const float* ga = reinterpret_cast<const float*>(sd.A) + c0;
+        for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) reinterpret_cast<float*>(sA)[i] = ga[i];
+      } else if constexpr (stage_a) {
         const double* ga = sd.A + c0;
         for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sA[i] = ga[i];
       }
     }
     __syncthreads();
-    if constexpr (CONV && !PAIRS) {
+    if constexpr (CONV) {
       // FP32 operator on FP64 values: each staged value is converted once,
       // in place, to a float pair (hi in the low word is the operator input).
       // MIX_S1 splits the accumulator exactly, hi + lo, and continues from
@@ -688,19 +707,17 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
           for (int i = 0; i < NP; i += 2) {
             OutT x0, x1 = OutT(0);
             double a0, a1 = 0.0;
-            epi_value<EPI, Real, OutT>(sd, stage_a ? sA[l0 + i * str] : 0.0, ku[i], x0, a0);
-            if (i + 1 < NP)
-              epi_value<EPI, Real, OutT>(sd, stage_a ? sA[l0 + (i + 1) * str] : 0.0, ku[i + 1], x1, a1);
+            epi_value<EPI, Real, OutT>(sd, aval(l0 + i * str), ku[i], x0, a0);
+            if (i + 1 < NP) epi_value<EPI, Real, OutT>(sd, aval(l0 + (i + 1) * str), ku[i + 1], x1, a1);
             if (paired) {
               if constexpr (EpiTraits<EPI>::writes_x) store2(static_cast<OutT*>(sd.Xout) + g0 + i, x0, x1);
-              store2(sd.Aout + g0 + i, a0, a1);
+              if constexpr (LO_OUT)
+                store2(reinterpret_cast<float*>(sd.Aout) + g0 + i, ff_lo(a0), ff_lo(a1));
+              else
+                store2(sd.Aout + g0 + i, a0, a1);
             } else {
-              if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g0 + i * str] = x0;
-              sd.Aout[g0 + i * str] = a0;
-              if (i + 1 < NP) {
-                if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g0 + (i + 1) * str] = x1;
-                sd.Aout[g0 + (i + 1) * str] = a1;
-              }
+              store_out(g0 + i * str, x0, a0);
+              if (i + 1 < NP) store_out(g0 + (i + 1) * str, x1, a1);
             }
           }
         }
@@ -724,9 +741,8 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
       const int lidx = cl * F * N + DIM * N + q;
       OutT xn;
       double an;
-      epi_value<EPI, Real, OutT>(sd, stage_a ? sA[lidx] : 0.0, k, xn, an);
-      if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
-      sd.Aout[g] = an;
+      epi_value<EPI, Real, OutT>(sd, aval(lidx), k, xn, an);
+      store_out(g, xn, an);
     }
     if (__syncthreads_or(!a_ok)) {
       // the accumulator copy timed out: stop as on an X time-out

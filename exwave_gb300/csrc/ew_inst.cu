@@ -76,7 +76,7 @@ template <typename Real, typename InT, int EPI>
 struct CartK {
   static constexpr bool SA = EpiTraits<EPI>::stage_a;
   static size_t smem(int cb, int sx) {
-    return CartSmem<DIM, NP, Real, InT, SlotOf<InT, EPI>>(cb, sx != 0, SA).end;
+    return CartSmem<DIM, NP, Real, InT, EpiTraits<EPI>::a_elem>(cb, sx != 0, SA).end;
   }
   static cudaError_t launch(const LaunchArgs& a, int sx, int tma, int grid, cudaStream_t st) {
     CartArgs ca;
@@ -143,7 +143,7 @@ void EW_TABLE_FN(KernelTable& t) {
   fill_cart<CartK<float, float, EPI_MIX_MID>>(t.cart[CV_MIX_MID]);
   fill_cart<CartK<float, float, EPI_MIX_LAST>>(t.cart[CV_MIX_LAST]);
   fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
-  fill_cart<CartK<float, double, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
+  fill_cart<CartK<float, float, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
   fill_cart<CartK<float, float, EPI_MIX_LAST_FF>>(t.cart[CV_MIX_LAST_FF]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
