@@ -216,14 +216,15 @@ def cpu_sample(degree, min_seconds=8.0):
 
 
 def traffic_from_profiles(precision, n_dofs):
-    """DRAM bytes per stage launch from the committed ncu summary, scaled to
-    this workload's DoF count (traffic grows in proportion to the cells)."""
+    """DRAM bytes per stage launch (average over the five stages of a
+    steady-state step) from the committed ncu summary, scaled to this
+    workload's DoF count (traffic grows in proportion to the cells)."""
     path = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
         e = d[precision]
-        return e["dram_bytes_per_dof_stage"] * n_dofs
+        return e["dram_bytes_per_dof_launch"] * n_dofs
     except (OSError, KeyError, ValueError):
         return None
 
@@ -471,8 +472,10 @@ def main():
     ms = float(t.item())
     ms_step = ms / args.steps
     value = n * STAGES * args.steps * ws / (ms / 1e3)
-    alg_bytes = BYTES_PER_DOF_STEP[args.precision] * n
-    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    # per launch of stage_cart_kernel: average algorithmic bytes of the five
+    # stages over the average launch duration (five launches per step)
+    alg_bytes = BYTES_PER_DOF_STEP[args.precision] * n / STAGES
+    achieved = alg_bytes / (ms_step / STAGES / 1e3) / 1e9
     traffic = traffic_from_profiles(args.precision, n)
     result = {
         "metric": "DoF-updates/s", "value": value, "unit": "DoF-updates/s", "n_gpus": ws,
@@ -488,8 +491,8 @@ def main():
         "api": "ew_lsrk45_steps (%d steps in one call)" % args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": traffic, "alg_bytes_per_step": alg_bytes,
-                     "kernel": "stage_kernel (5 launches per step)"},
+                     "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
+                     "launches_per_step": STAGES, "kernel": "stage_cart_kernel"},
         "errors": {"l2_p": errs[0], "l2_u": errs[1], "norm_p": errs[2]},
         "clocks": clk.summary(),
     }
