@@ -11,6 +11,12 @@
 // advances its clock.  The whole step is captured as a CUDA graph for each
 // parity of the state double buffer; membership changes rebuild tables and
 // graphs before the next step.
+//
+// Mixed precision keeps each solve's FP64 state in U[0] and, between the
+// steps, also its split into FP32 hi (stage input buffer X[parity]) and lo
+// (U[1], as floats): the first stage of a step reads hi and lo like a
+// middle stage reads its input, and the last stage writes the FP64 state
+// together with its split.  Receivers and get_state read the FP64 state.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,6 +29,7 @@
 
 #include "../../include/exwave_gb300.h"
 #include "ew_basis.h"
+#include "ew_device.cuh"
 #include "ew_internal.h"
 
 namespace {
@@ -136,6 +143,17 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity) {
   if (threadIdx.x == 0) {
     r.clock[0] += r.dt;
     r.clock[1] = (double)(step + 1);
+  }
+}
+
+// FP64 state -> FP32 hi and lo parts (hi + lo = state to about 48 bits).
+__global__ void split_state_kernel(const double* state, int64_t n, float* hi, float* lo) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float h, l;
+    ew::f64_split(state[i], h, l);
+    hi[i] = h;
+    lo[i] = l;
   }
 }
 
@@ -300,14 +318,18 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
   const double* A[5];
   void* Xo[5];
   double* Ao[5];
+  float* Lo = nullptr;
   if (b->mixed) {
-    void* X0 = s.X[0];
-    void* X1 = s.X[1];
-    X[0] = Nv; A[0] = Nv; Xo[0] = X0; Ao[0] = Pv;
-    X[1] = X0; A[1] = Pv; Xo[1] = X1; Ao[1] = Pv;
-    X[2] = X1; A[2] = Pv; Xo[2] = X0; Ao[2] = Pv;
-    X[3] = X0; A[3] = Pv; Xo[3] = X1; Ao[3] = Pv;
-    X[4] = X1; A[4] = Pv; Xo[4] = nullptr; Ao[4] = Pv;
+    // state U[0]; hi in X[parity], lo in U[1] (floats)
+    void* Xh = s.X[parity];
+    void* Xn = s.X[1 - parity];
+    double* S = s.U[0];
+    Lo = reinterpret_cast<float*>(s.U[1]);
+    X[0] = Xh; A[0] = reinterpret_cast<const double*>(Lo); Xo[0] = Xn; Ao[0] = S;
+    X[1] = Xn; A[1] = S; Xo[1] = Xh; Ao[1] = S;
+    X[2] = Xh; A[2] = S; Xo[2] = Xn; Ao[2] = S;
+    X[3] = Xn; A[3] = S; Xo[3] = Xh; Ao[3] = S;
+    X[4] = Xh; A[4] = S; Xo[4] = Xn; Ao[4] = S;
   } else {
     double* T = static_cast<double*>(s.X[0]);
     X[0] = Nv; A[0] = Nv; Xo[0] = T; Ao[0] = Pv;
@@ -323,6 +345,7 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
     d.A = A[st];
     d.Xout = Xo[st];
     d.Aout = Ao[st];
+    d.Lout = st == 4 ? Lo : nullptr;
     d.nbr = s.nbr;
     d.cellc = s.cellc;
     d.n_cells = s.n_cells;
@@ -369,11 +392,13 @@ int rebuild(ew_batch* b) {
     for (int d = 0; d < g.dim; ++d) N *= NP;
     const int F = g.dim + 1;
     for (int st = 0; st < 5; ++st) {
-      if (b->mixed)
-        g.variant[st] = st == 0 ? ew::CV_MIX_S1 : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST);
-      else
+      if (b->mixed) {
+        g.variant[st] = st == 0 ? ew::CV_MIX_S1_FF : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST_BOTH);
+        g.sx[st] = 1;
+      } else {
         g.variant[st] = st < 4 ? ew::CV_F64_MID : ew::CV_F64_LAST;
-      g.sx[st] = (st == 0) ? 0 : 1;  // first stage: X is the accumulator
+        g.sx[st] = (st == 0) ? 0 : 1;  // first stage: X is the accumulator
+      }
     }
     while (g.cb > 1 && kt.cart[g.variant[1]].smem(g.cb, 1) > 110 * 1024) --g.cb;
     const size_t cell_x = (size_t)F * N * (b->mixed ? 4 : 8);
@@ -430,7 +455,7 @@ int rebuild(ew_batch* b) {
       const Solve& s = b->solves[id];
       RecDesc r;
       r.U[0] = s.U[0];
-      r.U[1] = s.U[1];
+      r.U[1] = b->mixed ? s.U[0] : s.U[1];  // mixed: the FP64 state stays in U[0]
       r.rec_w = s.rec_w;
       r.rec_cell = s.rec_cell;
       r.trace = s.trace;
@@ -703,6 +728,10 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   up(s.rec_cell, reccell.data(), reccell.size() * 4);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.U[0], 0, (size_t)s.n_dofs * 8, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.U[1], 0, (size_t)s.n_dofs * 8, b->stream);
+  // mixed: the zero state's hi and lo parts
+  for (int k = 0; b->mixed && k < 2; ++k)
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.X[k], 0, (size_t)s.n_dofs * 4, b->stream);
+  if (b->mixed) s.cur = 0;
   if (e == cudaSuccess) e = cudaMemsetAsync(s.clock, 0, 16, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // host vectors go out of scope
   if (e != cudaSuccess) {
@@ -735,6 +764,14 @@ int ew_batch_set_state(ew_batch* b, int32_t id, const double* state) {
   if (s->steps_done != 0) return bfail(b, EW_ERR_INVALID, "set_state before the first step only");
   cudaError_t e = cudaMemcpyAsync(s->U[s->cur], state, (size_t)s->n_dofs * 8,
                                   cudaMemcpyDeviceToDevice, b->stream);
+  if (e == cudaSuccess && b->mixed) {
+    // hi and lo parts for the next first stage
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
+    split_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
+        s->U[0], s->n_dofs, static_cast<float*>(s->X[b->parity]), reinterpret_cast<float*>(s->U[1]));
+    e = cudaGetLastError();
+  }
   return e == cudaSuccess ? EW_OK : bcuda(b, e, "set state");
 }
 
@@ -779,7 +816,7 @@ int ew_batch_step(ew_batch* b, int32_t n_steps) {
   for (auto& kv : b->solves)
     if (kv.second.steps_done < kv.second.n_steps) {
       kv.second.steps_done += n_steps;
-      kv.second.cur ^= (n_steps & 1);
+      if (!b->mixed) kv.second.cur ^= (n_steps & 1);
       if (kv.second.steps_done >= kv.second.n_steps) finished = true;
     }
   // parity changed for everyone: solves keep their state in U[parity]

@@ -107,7 +107,14 @@ def test_batch_matches_single_context(env, precision):
     op.synchronize()
     b.synchronize()
     got = b.get_state(sid, torch.zeros_like(u0))
-    assert torch.equal(got, vn)
+    if precision == "fp64":
+        assert torch.equal(got, vn)
+    else:
+        # the batch carries the state's FP32 split between steps and runs
+        # other kernel instantiations, whose FP32 operations may round
+        # differently: agreement to FP32 round-off
+        err = ((got - vn).abs().max() / vn.abs().max()).item()
+        assert err < 1e-6, err
 
 
 def test_graphs_equal_direct_launches(env):
