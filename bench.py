@@ -383,8 +383,16 @@ def batch_workload(args, torch):
         seq_d += reqs[i].dofs() * 5 * args.steps
         one.close()
     sequential = seq_d / seq_t
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peak = float(json.load(f)["hbm_gbs"])
+    # algorithmic bytes of a step (each vector once per stage at its stored
+    # precision) over the step time, all groups together
+    achieved = BYTES_PER_DOF_STEP[args.precision] * dofs / (ms / args.steps / 1e3) / 1e9
     return {"metric": "DoF-updates/s (aggregate)", "value": batched, "unit": "DoF-updates/s",
             "ms_per_step": ms / args.steps, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": "measured",
+                         "kernel": "stage_cart_kernel (one launch per degree group and stage)"},
             "sequential_value": sequential, "batched_over_sequential": batched / sequential,
             "config": {"workload": "batch of %d 3-D solves (k 3..7, n 8..32, Ricker, 8 receivers)"
                                    % len(solves), "total_dofs": dofs, "precision": args.precision,

@@ -3,7 +3,7 @@
 For every (dimension, degree, precision) it builds a Cartesian membrane
 problem of about `target_dofs` DoFs, times LSRK45 steps with each admissible
 cells-per-block value (threads per block = cells x lines of the Cartesian
-kernel, at most 256) and keeps the fastest.  The table is written to
+kernel, at most 512) and keeps the fastest.  The table is written to
 exwave_gb300/tuning/tuning.json and loaded by the library at import
 (``ew_tune_set``), where ew_create and the batch runtime use it.
 
@@ -28,8 +28,8 @@ def lines_per_cell(dim, degree):
 
 
 def candidates(dim, degree):
-    lim = max(1, 256 // lines_per_cell(dim, degree))
-    c = sorted({1, 2, 3, 4, 6, 8, 12, 16, 24, 32, lim} & set(range(1, lim + 1)))
+    lim = max(1, 512 // lines_per_cell(dim, degree))
+    c = sorted({1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32, lim} & set(range(1, lim + 1)))
     return c
 
 
@@ -39,16 +39,14 @@ def time_case(dim, degree, precision, cells, cb, steps, torch):
     op = WaveEquationOperation(m, degree, precision=precision, cells_per_block=cb)
     u = op.project_membrane([1.0], [[1] * dim])
     v = torch.zeros_like(u)
-    op.lsrk45_step(dt, u, v)
+    stream = torch.cuda.current_stream()
+    op.set_stream(stream)
+    op.lsrk45_steps(dt, 1, u, v)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    stream = torch.cuda.current_stream()
-    op.set_stream(stream)
     e0.record(stream)
-    for _ in range(steps):
-        op.lsrk45_step(dt, u, v)
-        u, v = v, u
+    op.lsrk45_steps(dt, steps, v, u)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)

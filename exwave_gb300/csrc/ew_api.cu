@@ -752,7 +752,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     const int tuned = ew::tuned_cells_per_block(c->dim, c->degree, opt.precision);
     c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block
                                          : (tuned > 0 ? tuned : std::max(1, 256 / lines));
-    c->cb_cart = std::max(1, std::min(c->cb_cart, 256 / lines));
+    c->cb_cart = std::max(1, std::min(c->cb_cart, std::max(1, 512 / lines)));
     const int v = c->mixed ? ew::CV_MIX_MID : ew::CV_F64_MID;
     while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1) > 110 * 1024) --c->cb_cart;
   }

@@ -386,7 +386,7 @@ int rebuild(ew_batch* b) {
     const ew::KernelTable& kt = ew::kernel_table(g.dim, g.np);
     const int lines = kt.lines;
     const int tuned = ew::tuned_cells_per_block(g.dim, g.np - 1, b->mixed ? 1 : 0);
-    g.cb = tuned > 0 ? std::min(tuned, std::max(1, 256 / lines)) : std::max(1, 256 / lines);
+    g.cb = tuned > 0 ? std::min(tuned, std::max(1, 512 / lines)) : std::max(1, 256 / lines);
     const int NP = g.np;
     int N = 1;
     for (int d = 0; d < g.dim; ++d) N *= NP;

@@ -142,7 +142,9 @@ class Server:
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "admission_wait_p50_s": float(np.percentile(wait, 50)) if len(wait) else None,
-            "backlog_at_end": len(queue) + len(pending), "active_at_end": len(active),
+            # arrived but not yet admitted / not yet arrived when the run stopped
+            "backlog_at_end": len(queue), "not_arrived_at_end": len(pending),
+            "active_at_end": len(active),
             "peak_active": peak_active, "ticks": ticks,
             "dof_updates_per_s": dof_updates / wall if wall > 0 else 0.0,
         }
