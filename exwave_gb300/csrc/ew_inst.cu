@@ -4,6 +4,7 @@
 #include "ew_cart.cuh"
 #include "ew_kernels.cuh"
 #include "ew_launch.h"
+#include "ew_stage_tma.cuh"
 
 #ifndef EW_DIM
 #error "EW_DIM must be defined"
@@ -51,11 +52,32 @@ int blocks_per_sm(Kern kern, int block, size_t smem) {
 template <typename Real, typename InT, typename OutT, bool CART>
 struct StageK {
   static size_t smem(int cb) { return (size_t)OpSmem<DIM, NP, CART>(cb).end * sizeof(Real); }
+  static size_t smem_staged(int cb) { return StagedSmem<DIM, NP>(cb, (int)sizeof(Real)).end; }
+  // The staged kernel (bulk copies) serves curved cells when the input is
+  // already in the compute type and every per-cell block is a multiple of
+  // 16 bytes; the pointers are checked at launch.
+  static bool staged_ok(int cb) {
+    constexpr size_t F = DIM + 1;
+    return !CART && std::is_same<Real, InT>::value && (F * N * sizeof(Real)) % 16 == 0 &&
+           (F * N * 8) % 16 == 0 && ((size_t)(1 << DIM) * DIM * sizeof(Real)) % 16 == 0 &&
+           2 * DIM <= N && smem_staged(cb) <= 220 * 1024;
+  }
+  static bool aligned(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
   static cudaError_t launch(const LaunchArgs& a, int grid, cudaStream_t st) {
     const int cb = a.cells_per_block;
+    if constexpr (!CART && std::is_same<Real, InT>::value) {
+      const SolveDesc& s = a.single;
+      if (staged_ok(cb) && a.solves == nullptr && aligned(s.X) && aligned(s.geo) && aligned(s.mat) &&
+          (s.mode == MODE_APPLY || aligned(s.A)))
+        return run(stage_kernel_staged<DIM, NP, Real, OutT>, a, grid, cb * N, smem_staged(cb), st);
+    }
     return run(stage_kernel<DIM, NP, Real, InT, OutT, CART>, a, grid, cb * N, smem(cb), st);
   }
   static int occupancy(int cb) {
+    if constexpr (!CART && std::is_same<Real, InT>::value) {
+      if (staged_ok(cb))
+        return blocks_per_sm(stage_kernel_staged<DIM, NP, Real, OutT>, cb * N, smem_staged(cb));
+    }
     return blocks_per_sm(stage_kernel<DIM, NP, Real, InT, OutT, CART>, cb * N, smem(cb));
   }
 };
