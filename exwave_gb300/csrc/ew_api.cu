@@ -642,15 +642,23 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     return code;
   };
 
-  // geometry: Cartesian cells keep their extents, others their vertices
+  // geometry: Cartesian cells keep their extents, others the monomial
+  // coefficients of their multilinear map (inclusion-exclusion over the
+  // vertices, in FP64: C_S = sum_{T subset S} (-1)^{|S|-|T|} V_T)
   const int geo_per_cell = cart ? dim : nv * dim;
   std::vector<double> geo((size_t)c->n_cells * geo_per_cell);
   for (int64_t i = 0; i < c->n_cells; ++i) {
     const double* V = mesh->vertices + (size_t)i * nv * dim;
-    if (cart)
+    if (cart) {
       for (int e = 0; e < dim; ++e) geo[i * dim + e] = V[(nv - 1) * dim + e] - V[e];
-    else
-      std::copy(V, V + nv * dim, geo.begin() + i * nv * dim);
+    } else {
+      double* C = geo.data() + (size_t)i * nv * dim;
+      std::copy(V, V + nv * dim, C);
+      for (int d = 0; d < dim; ++d)
+        for (int S = 0; S < nv; ++S)
+          if ((S >> d) & 1)
+            for (int e = 0; e < dim; ++e) C[S * dim + e] -= C[(S ^ (1 << d)) * dim + e];
+    }
   }
   // per cell: rho, c, tau = 1/(c rho), 1/rho
   std::vector<double> mat((size_t)c->n_cells * 4);
@@ -742,7 +750,8 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   if (ce != cudaSuccess) return bail(cuda_fail(c, ce, "constant upload"));
   // work lists and persistent grid sizes
   c->cb_stage = default_cb(c->N, opt.cells_per_block);
-  c->cb_ck = c->cb_stage;
+  // mixed CK kernel: 80 registers a thread, two blocks per SM need 384 threads or fewer
+  c->cb_ck = c->mixed ? std::max(1, std::min(c->cb_stage, 384 / c->N)) : c->cb_stage;
   const int ck_var = c->mixed ? 1 : 0;
   while (c->cb_ck > 1 &&
          c->kt->ck[ck_var][cart][c->post].smem(c->cb_ck) > 200 * 1024)

@@ -46,7 +46,8 @@ struct SolveDesc {
   void* Xout;          // next stage input (OutT), MODE_RK_MID
   double* Aout;        // MODE_APPLY: result; RK modes: accumulator out (may alias A)
   const int32_t* nbr;  // [cell][2*DIM]
-  const void* geo;     // Real: Cartesian [cell][DIM] extents; else [cell][2^DIM][DIM] vertices
+  const void* geo;     // Real: Cartesian [cell][DIM] extents; else [cell][2^DIM][DIM] monomial
+                       // coefficients of the multilinear map (see geom_general)
   const void* mat;     // Real [cell][2] = (rho, c)
   int64_t n_cells;
   double f1, f2;
@@ -205,10 +206,15 @@ __device__ __forceinline__ T load_nc(const T* p) {
 }
 
 // ---------------------------------------------------------------- geometry
-// Multilinear cell map from 2^DIM vertices (deal.II lexicographic order).
-// Returns det J and fills JiT[d][e] = d xi_e / d x_d.
+// Multilinear cell map in monomial form: x(xi) = sum_S C_S prod_{d in S} xi_d
+// over the subsets S of the DIM directions (bit masks), C_S[i] at
+// C[S * DIM + i]; the host derives C from the 2^DIM vertices (deal.II
+// lexicographic order) by C_S = sum_{T subset S} (-1)^{|S|-|T|} V_T.
+// dx/dxi_j then needs one FMA per term: about 40 operations for J in 3-D
+// instead of 120 from the vertices.  Returns det J and fills
+// JiT[d][e] = d xi_e / d x_d.
 template <int DIM, typename Real>
-__device__ __forceinline__ Real geom_general(const Real* V, const Real* xi, Real JiT[DIM][DIM]) {
+__device__ __forceinline__ Real geom_general(const Real* C, const Real* xi, Real JiT[DIM][DIM]) {
   constexpr int NV = 1 << DIM;
   Real J[DIM][DIM];
 #pragma unroll
@@ -216,15 +222,16 @@ __device__ __forceinline__ Real geom_general(const Real* V, const Real* xi, Real
 #pragma unroll
     for (int j = 0; j < DIM; ++j) J[i][j] = Real(0);
 #pragma unroll
-  for (int v = 0; v < NV; ++v) {
+  for (int S = 1; S < NV; ++S) {
 #pragma unroll
     for (int j = 0; j < DIM; ++j) {
-      Real dphi = ((v >> j) & 1) ? Real(1) : Real(-1);
+      if (!((S >> j) & 1)) continue;
+      Real prod = Real(1);
 #pragma unroll
-      for (int e = 0; e < DIM; ++e)
-        if (e != j) dphi *= ((v >> e) & 1) ? xi[e] : Real(1) - xi[e];
+      for (int d = 0; d < DIM; ++d)
+        if (d != j && ((S >> d) & 1)) prod *= xi[d];
 #pragma unroll
-      for (int i = 0; i < DIM; ++i) J[i][j] += V[v * DIM + i] * dphi;
+      for (int i = 0; i < DIM; ++i) J[i][j] += C[S * DIM + i] * prod;
     }
   }
   if constexpr (DIM == 2) {

@@ -615,7 +615,7 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Real* c0) {
 }
 
 template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST>
-__global__ void __launch_bounds__(512) ck_kernel(const LaunchArgs La) {
+__global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const LaunchArgs La) {
   using S = Shape<DIM, NP, CART>;
   constexpr int F = S::F, N = S::N;
   constexpr int NL = n_levels(NP);
