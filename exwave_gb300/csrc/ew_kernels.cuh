@@ -55,9 +55,11 @@ template <int DIM, int NP, bool CART>
 struct CkSmem {
   using S = Shape<DIM, NP, CART>;
   OpSmem<DIM, NP, CART> op;
-  int Sv, T1, T2, C[8], end;
+  int Sv, T1, T2, C[8], J, end;
   __host__ __device__ explicit CkSmem(int CB) : op(CB) {
-    Sv = op.end;
+    // J: inverse-transpose Jacobians at the level-0 points, [cell][DIM*DIM][point]
+    J = op.end;
+    Sv = J + (CART ? 0 : CB * DIM * DIM * S::N);
     T1 = Sv + CB * S::F * S::N;
     T2 = T1 + CB * S::F * S::N;
     int o = T2 + CB * S::F * S::N;
@@ -489,7 +491,8 @@ __device__ __forceinline__ void tensor_ct(const Real* Mtx, const Real* src, int 
 // (integrate_taylor_cauchykovalewski_step, wave_equation_operations.cc:1096-1197).
 template <int DIM, int M, typename Real, bool CART>
 __device__ __forceinline__ void ck_deriv(const Real* D, const Real* x, const Real* Sv,
-                                         const Real* sGeo, Real rho, Real c_sq, int qq, Real* out) {
+                                         const Real* sGeo, Real rho, Real c_sq, int qq, Real* out,
+                                         const Real* sJ = nullptr) {
   constexpr int NM = ipow_c(M, DIM);
   int i[3] = {0, 0, 0};
   i[0] = qq % M;
@@ -515,7 +518,15 @@ __device__ __forceinline__ void ck_deriv(const Real* D, const Real* x, const Rea
 #pragma unroll
   for (int e = 0; e < DIM; ++e) xi[e] = x[i[e]];
   Real JiT[DIM][DIM];
-  cell_geom<DIM, Real, CART>(sGeo, xi, JiT);
+  if (sJ) {
+    // cached at this point: [DIM*DIM][M^DIM] of the cell
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int e = 0; e < DIM; ++e) JiT[d][e] = sJ[(d * DIM + e) * NM + qq];
+  } else {
+    cell_geom<DIM, Real, CART>(sGeo, xi, JiT);
+  }
   Real div = Real(0);
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
@@ -540,6 +551,7 @@ struct CkState {
   Real* sT1;
   Real* sT2;
   Real* sm;
+  const Real* sJ;  // level-0 Jacobian cache of the item (nullptr: none)
   const int* C;  // level contribution offsets (in units of Real)
   const Real* sGeo;
   int cl, q, nc;
@@ -563,7 +575,8 @@ __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Rea
   const bool act = st.active && st.q < NM;
   if (act)
     ck_deriv<DIM, M, Real, CART>(L.D, L.x, st.sS + st.cl * F * N, st.sGeo + st.cl * GEO, st.rho,
-                                 st.c_sq, st.q, sn);
+                                 st.c_sq, st.q, sn,
+                                 (R == 0 && st.sJ) ? st.sJ + st.cl * DIM * DIM * N : nullptr);
   __syncthreads();
   if (act) {
     const Real f = fac[S];
@@ -671,6 +684,25 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     const Real rho = active ? sMat[4 * cl] : Real(1);
     const Real cc = active ? sMat[4 * cl + 1] : Real(1);
     const Real c_sq = cc * cc;
+    // inverse-transpose Jacobian at this thread's level-0 point, evaluated
+    // once and read back (by this thread only) by every level-0 derivative
+    Real* sJ = CART ? nullptr : sm + lay.J;
+    if constexpr (!CART) {
+      if (active) {
+        const Level<Real> L0 = get_level(sB, NP, 0);
+        int i[3] = {0, 0, 0};
+        split_point<DIM, NP>(q, i);
+        Real xi[DIM];
+#pragma unroll
+        for (int e = 0; e < DIM; ++e) xi[e] = L0.x[i[e]];
+        Real JiT[DIM][DIM];
+        cell_geom<DIM, Real, false>(sGeo + cl * S::GEO, xi, JiT);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+#pragma unroll
+          for (int e = 0; e < DIM; ++e) sJ[(cl * DIM * DIM + d * DIM + e) * N + q] = JiT[d][e];
+      }
+    }
     Real d1[F];
     if constexpr (POST) {
       // first time derivative = full DG operator (recongraddiv = apply(src))
@@ -687,7 +719,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
         Real o[F];
         const Level<Real> L0 = get_level(sB, NP, 0);
         ck_deriv<DIM, NP, Real, CART>(L0.D, L0.x, sX + cl * F * N, sGeo + cl * S::GEO, rho, c_sq,
-                                      q, o);
+                                      q, o, CART ? nullptr : sJ + cl * DIM * DIM * N);
 #pragma unroll
         for (int fld = 0; fld < F; ++fld) d1[fld] = -o[fld];
       }
@@ -709,6 +741,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     st.sT1 = sm + lay.T1;
     st.sT2 = sm + lay.T2;
     st.sm = sm;
+    st.sJ = sJ;
     st.C = lay.C;
     st.sGeo = sGeo;
     st.cl = cl;
