@@ -54,9 +54,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="membrane3d",
-                    choices=["membrane3d", "ader3d", "batch", "serve", "sweep"],
-                    help="membrane3d (default headline), ader3d (curved two-layer ADER), batch "
-                         "(512 independent solves), serve (continuous batching), sweep (degrees)")
+                    choices=["membrane3d", "membrane2d", "ader3d", "batch", "serve", "sweep"],
+                    help="membrane3d (default headline), membrane2d (2-D 16^2 k=4 to T=1), ader3d "
+                         "(curved two-layer ADER), batch (512 independent solves), serve "
+                         "(continuous batching), sweep (degrees)")
     ap.add_argument("--solves", type=int, default=512)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--time-limit", type=float, default=60.0)
@@ -332,6 +333,49 @@ def ader3d(args, torch):
                        "n_dofs": opm.n_dofs, "dt": dt, "x0": x0}}
 
 
+def membrane2d(args, torch):
+    """2-D vibrating membrane, 16^2 affine quads, FE_DGQ(4), modes (1,1) +
+    0.5 (2,3), p = 0 on the boundary, LSRK45 with dt = 2^-9, 512 steps to
+    T = 1, FP64 and mixed: time of the whole run (one ew_lsrk45_steps call)
+    and L2 errors against the analytic solution."""
+    import exwave_gb300 as ew
+    amps, kvecs = [1.0, 0.5], [[1, 1], [2, 3]]
+    m = ew.hypercube(2, 16, 0, 0.0, boundary_ids=2)
+    dt = ew.time_step_size(m, 0.25 / 4 ** 1.5)
+    steps = int(round(1.0 / dt))
+    out, states = {}, {}
+    for prec in ("mixed", "fp64"):
+        op = ew.WaveEquationOperation(m, 4, precision=prec)
+        stream = torch.cuda.current_stream()
+        op.set_stream(stream)
+        u0 = op.project_membrane(amps, kvecs, 0.0)
+        u, v = u0.clone(), torch.zeros_like(u0)
+        op.lsrk45_steps(dt, args.warmup, u, v)  # warm-up (discarded)
+        u, v = u0.clone(), torch.zeros_like(u0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        op.lsrk45_steps(dt, steps, u, v)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        err = op.l2_errors(v, amps, kvecs, steps * dt)
+        out[prec] = {"value": op.n_dofs * STAGES * steps / (ms / 1e3), "ms_total": ms,
+                     "l2_p": err[0], "l2_u": err[1], "norm_p": err[2]}
+        states[prec] = (op, v)
+    op64, v64 = states["fp64"]
+    diff = op64.l2_difference(states["mixed"][1], v64)
+    return {"metric": "DoF-updates/s", "value": out["mixed"]["value"], "unit": "DoF-updates/s",
+            "mixed": out["mixed"], "fp64": out["fp64"],
+            "error_ratio_p": out["mixed"]["l2_p"] / out["fp64"]["l2_p"],
+            "error_ratio_u": out["mixed"]["l2_u"] / out["fp64"]["l2_u"],
+            "mixed_vs_fp64_l2": {"p": diff[0], "u": diff[1]},
+            "config": {"workload": "2-D vibrating membrane, 16^2 affine quads, FE_DGQ(4), LSRK45, "
+                                   "512 steps to T=1", "n_dofs": op64.n_dofs, "dt": dt,
+                       "steps": steps, "note": "launch-bound at this size (19,200 DoFs)"}}
+
+
 def batch_workload(args, torch):
     """Batch of independent 3-D solves drawn from a seed (degree uniform in
     {3..7}, n^3 cells n in [8,32], c ~ U[1,4], rho ~ U[1,3], Ricker source
@@ -442,7 +486,7 @@ def main():
         from exwave_gb300 import build
         build.build()
         fn = {"ader3d": ader3d, "batch": batch_workload, "serve": serve_workload,
-              "sweep": sweep_workload}[args.workload]
+              "sweep": sweep_workload, "membrane2d": membrane2d}[args.workload]
         with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
             res = fn(args, torch)
         res["clocks"] = clk.summary()
