@@ -273,7 +273,10 @@ def ader3d(args, torch):
     """ADER of order k+1, 3-D k=4, 40^3 hexes on the curved mesh x_i += 0.03
     prod_d sin(2 pi x_d), two layers split at z = 0.5 (c=1, rho=1 below; c=3,
     rho=2 above), Gaussian pulse (width 0.05) at a seeded point of the lower
-    layer, p = 0 on the top face, rigid walls elsewhere; CFL 0.2."""
+    layer, p = 0 on the top face, rigid walls elsewhere; CFL 0.15.  (CFL
+    0.2, the value of the reference's 3-D ADER test, is unstable on this
+    curved mesh from 24^3 cells on: the oracle, the reference algorithm on
+    the CPU, grows exactly like the GPU path from a random state.)"""
     import numpy as np
     import exwave_gb300 as ew
     k, n = 4, (args.cells if args.cells != 64 else 40)
@@ -281,7 +284,8 @@ def ader3d(args, torch):
     ew.layered_materials(m, 0.5, below=(1.0, 1.0), above=(3.0, 2.0))
     rng = np.random.default_rng(2024)
     x0 = [rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.15, 0.35)]
-    dt = ew.time_step_size(m, 0.2 / k ** 1.5)
+    cfl = 0.15
+    dt = ew.time_step_size(m, cfl / k ** 1.5)
     out = {}
     states = {}
     for prec in ("mixed", "fp64"):
@@ -309,28 +313,48 @@ def ader3d(args, torch):
                      "gpu_launches": op.kernel_launches() - l0}
         op.synchronize()
         states[prec] = (op, u, steps)
-    # same number of steps on both paths for the comparison
-    n_cmp = states["fp64"][2] + args.warmup
-    opm = ew.WaveEquationOperation(m, k, precision="mixed")
-    um = opm.project_gaussian(x0, 0.05)
-    vm = torch.zeros_like(um)
-    op64 = ew.WaveEquationOperation(m, k, precision="fp64")
-    u64 = op64.project_gaussian(x0, 0.05)
-    v64 = torch.zeros_like(u64)
-    for _ in range(n_cmp):
-        opm.ader_step(dt, um, vm)
-        um, vm = vm, um
-        op64.ader_step(dt, u64, v64)
-        u64, v64 = v64, u64
-    diff = op64.l2_difference(um, u64)
+    # the configuration's run to T = 0.5 on both paths, with 8 seeded
+    # receivers sampled every step: final-state and receiver-trace errors of
+    # the mixed path against FP64
+    rec = np.random.default_rng(2025).uniform(0.1, 0.9, (8, 3))
+    t_end = 0.5
+    n_steps = int(np.ceil(t_end / dt - 1e-12))
+    finals, traces, run_ms = {}, {}, {}
+    for prec in ("mixed", "fp64"):
+        op = ew.WaveEquationOperation(m, k, precision=prec)
+        stream = torch.cuda.current_stream()
+        op.set_stream(stream)
+        op.set_receivers(rec)
+        u = op.project_gaussian(x0, 0.05)
+        v = torch.zeros_like(u)
+        trace = torch.zeros(n_steps + 1, 8 * 4, dtype=torch.float64, device="cuda")
+        op.sample_receivers(u, trace[0])
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(n_steps):
+            op.ader_step(dt, u, v)
+            u, v = v, u
+            op.sample_receivers(u, trace[s + 1])
+        e1.record(stream)
+        op.synchronize()
+        run_ms[prec] = e0.elapsed_time(e1)
+        finals[prec] = (op, u)
+        traces[prec] = trace.view(n_steps + 1, 8, 4)[:, :, 3].cpu().numpy()
+    op64, u64 = finals["fp64"]
+    diff = op64.l2_difference(finals["mixed"][1], u64)
     ref = op64.l2_difference(u64, torch.zeros_like(u64))
+    tr_err = float(np.abs(traces["mixed"] - traces["fp64"]).max() / np.abs(traces["fp64"]).max())
     return {"metric": "DoF-updates/s (ADER: 1 per DoF and step)", "value": out["mixed"]["value"],
             "unit": "DoF-updates/s", "ms_per_step": out["mixed"]["ms_per_step"],
             "fp64": out["fp64"], "gpu_launches": out["mixed"]["gpu_launches"],
-            "mixed_vs_fp64_rel_l2_p": diff[0] / ref[0], "mixed_vs_fp64_rel_l2_u":
-            diff[1] / max(ref[1], 1e-300), "compare_steps": n_cmp,
+            "run_to_T": {"t_end": n_steps * dt, "steps": n_steps, "mixed_ms": run_ms["mixed"],
+                         "fp64_ms": run_ms["fp64"],
+                         "mixed_vs_fp64_rel_l2_p": diff[0] / ref[0],
+                         "mixed_vs_fp64_rel_l2_u": diff[1] / max(ref[1], 1e-300),
+                         "receiver_trace_rel_err_p": tr_err, "receivers": rec.tolist()},
             "config": {"workload": "ADER k=4 3-D 40^3 curved two-layer Gaussian pulse",
-                       "n_dofs": opm.n_dofs, "dt": dt, "x0": x0}}
+                       "n_dofs": op64.n_dofs, "dt": dt, "cfl": cfl, "x0": x0}}
 
 
 def membrane2d(args, torch):

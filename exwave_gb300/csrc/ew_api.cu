@@ -326,6 +326,10 @@ struct ew_ctx {
   double* d_acc = nullptr;
   double* d_l2 = nullptr;  // interp (m x np), qx (m), qw (m)
   int l2_m = 0;
+  // receivers (ew_set_receivers): cell and N interpolation weights each
+  int32_t n_rec = 0;
+  int32_t* d_rec_cell = nullptr;
+  double* d_rec_w = nullptr;
   std::string last_error;
   int64_t launches = 0;
 };
@@ -369,7 +373,7 @@ void free_ctx(ew_ctx* c) {
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
                   c->d_work_stage, c->d_work_ck, c->d_work_cart, c->d_cellc, c->d_err, c->d_tmp64, c->d_x32[0],
-                  c->d_x32[1], c->d_acc, c->d_l2};
+                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -586,6 +590,84 @@ int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
 }  // namespace
 
 // ================================================================ C ABI
+// ---- receivers (helpers) ---------------------------------------------------------------
+namespace {
+// Multilinear map of a cell (2^dim vertices, lexicographic) and its Jacobian.
+void cell_map(int dim, const double* V, const double* xi, double* x, double* J) {
+  const int nv = 1 << dim;
+  for (int i = 0; i < dim; ++i) {
+    x[i] = 0.0;
+    for (int j = 0; j < dim; ++j) J[i * dim + j] = 0.0;
+  }
+  for (int v = 0; v < nv; ++v) {
+    double phi = 1.0;
+    for (int d = 0; d < dim; ++d) phi *= ((v >> d) & 1) ? xi[d] : 1.0 - xi[d];
+    for (int i = 0; i < dim; ++i) x[i] += V[v * dim + i] * phi;
+    for (int j = 0; j < dim; ++j) {
+      double dp = ((v >> j) & 1) ? 1.0 : -1.0;
+      for (int d = 0; d < dim; ++d)
+        if (d != j) dp *= ((v >> d) & 1) ? xi[d] : 1.0 - xi[d];
+      for (int i = 0; i < dim; ++i) J[i * dim + j] += V[v * dim + i] * dp;
+    }
+  }
+}
+
+// Reference coordinates of point p in a cell by Newton's method on the
+// multilinear map; true if p lies in the cell (with a small tolerance).
+bool invert_map(int dim, const double* V, const double* p, double* xi) {
+  for (int d = 0; d < dim; ++d) xi[d] = 0.5;
+  double x[3], J[9];
+  for (int it = 0; it < 40; ++it) {
+    cell_map(dim, V, xi, x, J);
+    double r[3], dx[3] = {0, 0, 0};
+    for (int i = 0; i < dim; ++i) r[i] = x[i] - p[i];
+    if (dim == 2) {
+      const double det = J[0] * J[3] - J[1] * J[2];
+      if (det == 0.0) return false;
+      dx[0] = (J[3] * r[0] - J[1] * r[1]) / det;
+      dx[1] = (-J[2] * r[0] + J[0] * r[1]) / det;
+    } else {
+      const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
+                   c02 = J[3] * J[7] - J[4] * J[6];
+      const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+      if (det == 0.0) return false;
+      // inverse = adj(J) / det, adj = cofactor matrix transposed
+      const double c10 = J[2] * J[7] - J[1] * J[8], c11 = J[0] * J[8] - J[2] * J[6],
+                   c12 = J[1] * J[6] - J[0] * J[7];
+      const double c20 = J[1] * J[5] - J[2] * J[4], c21 = J[2] * J[3] - J[0] * J[5],
+                   c22 = J[0] * J[4] - J[1] * J[3];
+      dx[0] = (c00 * r[0] + c10 * r[1] + c20 * r[2]) / det;
+      dx[1] = (c01 * r[0] + c11 * r[1] + c21 * r[2]) / det;
+      dx[2] = (c02 * r[0] + c12 * r[1] + c22 * r[2]) / det;
+    }
+    double step = 0.0;
+    for (int d = 0; d < dim; ++d) {
+      xi[d] -= dx[d];
+      step = std::max(step, std::fabs(dx[d]));
+    }
+    if (step < 1e-14) break;
+  }
+  for (int d = 0; d < dim; ++d)
+    if (!(xi[d] >= -1e-10 && xi[d] <= 1.0 + 1e-10)) return false;
+  return true;
+}
+
+// One warp per receiver: every field of the state at the receiver.
+__global__ void receivers_kernel(const double* state, int n, int F, int N, const int32_t* cell,
+                                 const double* w, double* out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* wr = w + (size_t)warp * N;
+  for (int fld = 0; fld < F; ++fld) {
+    const double* s = state + ((size_t)cell[warp] * F + fld) * N;
+    double acc = 0.0;
+    for (int q = lane; q < N; q += 32) acc += wr[q] * s[q];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[(size_t)warp * F + fld] = acc;
+  }
+}
+}  // namespace
+
 extern "C" {
 
 const char* ew_last_error(const ew_ctx* ctx) {
@@ -1156,6 +1238,73 @@ int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_pe
 
 int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision) {
   return ew::tuned_cells_per_block(dim, degree, precision);
+}
+
+int ew_set_receivers(ew_ctx* ctx, int32_t n, const double* points) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && !points)) return fail(ctx, EW_ERR_INVALID, "ew_set_receivers: invalid points");
+  const int dim = ctx->dim, nv = 1 << dim, N = ctx->N;
+  std::vector<double> verts((size_t)ctx->n_cells * nv * dim);
+  cudaError_t e = cudaMemcpy(verts.data(), ctx->d_verts, verts.size() * 8, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "vertex readback");
+  const ew::GaussRule g = ew::gauss_rule(ctx->np);
+  std::vector<int32_t> cells(std::max(n, 1), 0);
+  std::vector<double> w((size_t)std::max(n, 1) * N, 0.0);
+  for (int r = 0; r < n; ++r) {
+    const double* p = points + (size_t)r * dim;
+    int32_t found = -1;
+    double xi[3] = {0, 0, 0};
+    for (int64_t c = 0; c < ctx->n_cells && found < 0; ++c) {
+      const double* V = verts.data() + (size_t)c * nv * dim;
+      bool inbox = true;
+      for (int d = 0; d < dim && inbox; ++d) {
+        double lo = V[d], hi = V[d];
+        for (int v = 1; v < nv; ++v) {
+          lo = std::min(lo, V[v * dim + d]);
+          hi = std::max(hi, V[v * dim + d]);
+        }
+        const double tol = 1e-10 * (hi - lo);
+        inbox = p[d] >= lo - tol && p[d] <= hi + tol;
+      }
+      if (inbox && invert_map(dim, V, p, xi)) found = (int32_t)c;
+    }
+    if (found < 0) return fail(ctx, EW_ERR_INVALID, "ew_set_receivers: point " + std::to_string(r) + " is outside the mesh");
+    cells[r] = found;
+    for (int q = 0; q < N; ++q) {
+      double v = 1.0;
+      int t = q;
+      for (int d = 0; d < dim; ++d) {
+        v *= ew::lagrange(g.x, t % ctx->np, std::min(1.0, std::max(0.0, xi[d])));
+        t /= ctx->np;
+      }
+      w[(size_t)r * N + q] = v;
+    }
+  }
+  if (ctx->d_rec_cell) cudaFree(ctx->d_rec_cell);
+  if (ctx->d_rec_w) cudaFree(ctx->d_rec_w);
+  ctx->d_rec_cell = nullptr;
+  ctx->d_rec_w = nullptr;
+  ctx->n_rec = 0;
+  if ((rc = dev_alloc(ctx, &ctx->d_rec_cell, cells.size())) || (rc = dev_alloc(ctx, &ctx->d_rec_w, w.size())) ||
+      (rc = upload(ctx, ctx->d_rec_cell, cells.data(), cells.size() * 4)) ||
+      (rc = upload(ctx, ctx->d_rec_w, w.data(), w.size() * 8)))
+    return rc;
+  ctx->n_rec = n;
+  return EW_OK;
+}
+
+int ew_sample_receivers(ew_ctx* ctx, const double* state, double* out) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!state || !out) return fail(ctx, EW_ERR_INVALID, "ew_sample_receivers: NULL vector");
+  if (ctx->n_rec == 0) return EW_OK;
+  const int threads = 256, per_block = threads / 32;
+  receivers_kernel<<<(ctx->n_rec + per_block - 1) / per_block, threads, 0, ctx->stream>>>(
+      state, ctx->n_rec, ctx->F, ctx->N, ctx->d_rec_cell, ctx->d_rec_w, out);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "receiver launch");
 }
 
 int ew_synchronize(ew_ctx* ctx) {

@@ -108,6 +108,21 @@ class WaveEquationOperation:
         """n_steps LSRK45 steps in one call (vec_n in, clobbered; vec_np out)."""
         self._chk(self.L.ew_lsrk45_steps(self.ctx, dt, int(n_steps), _ptr(vec_n), _ptr(vec_np)))
 
+    def set_receivers(self, points):
+        """Locate receiver points (array n x dim) once."""
+        p = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, self.dim))
+        self._chk(self.L.ew_set_receivers(self.ctx, p.shape[0], p.ctypes.data))
+        self.n_receivers = p.shape[0]
+
+    def sample_receivers(self, state, out=None):
+        """Fields at the receivers: a (n, dim + 1) device tensor (or a view of
+        `out`, e.g. one row of a preallocated trace)."""
+        if out is None:
+            out = self.torch.zeros(self.n_receivers * (self.dim + 1), dtype=self.torch.float64,
+                                   device="cuda:%d" % self.device)
+        self._chk(self.L.ew_sample_receivers(self.ctx, _ptr(state), _ptr(out)))
+        return out.view(self.n_receivers, self.dim + 1)
+
     def ader_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_ader_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 

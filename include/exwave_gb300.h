@@ -126,6 +126,19 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
  * the final state is FP64. */
 int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, double* vec_np);
 
+/* Receivers: point evaluation of the solution, the data a time_step_analysis
+ * hook (utilities.h:136-142) records at fixed points.  ew_set_receivers
+ * locates n points (host array, n x dim, physical coordinates) once: the
+ * containing cell and the reference coordinates (Newton's method on the
+ * multilinear map), then the Lagrange weights of the Gauss-point basis.
+ * EW_ERR_INVALID names the first point outside the mesh.  Replaces any
+ * earlier set. */
+int ew_set_receivers(ew_ctx* ctx, int32_t n, const double* points);
+
+/* Every field (u_0..u_{d-1}, p) of a device state at the receivers into the
+ * device array out (n x (dim+1), receiver-major), on the context's stream. */
+int ew_sample_receivers(ew_ctx* ctx, const double* state, double* out);
+
 /* The same LSRK45 step as ew_lsrk45_step, for callers that cannot have the
  * library allocate device memory: it has no counterpart in the reference.
  * Code that runs the step inside an application which owns all device
