@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--solves", type=int, default=512)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--time-limit", type=float, default=60.0)
+    ap.add_argument("--degrees", default="3,7", help="batch: degree range (inclusive)")
+    ap.add_argument("--sizes", default="8,32", help="batch: cells per direction range (inclusive)")
     ap.add_argument("--quick", action="store_true",
                     help="ader3d: timing only, without the run to T=0.5 on both paths")
     return ap.parse_args()
@@ -417,7 +419,9 @@ def batch_workload(args, torch):
     import numpy as np
     from exwave_gb300 import serve
     from exwave_gb300.batch import Batch
-    reqs = serve.draw_requests(args.solves, rate=0.0, seed=7, end_time=(1.0, 1.0))
+    dg = tuple(int(x) for x in args.degrees.split(","))
+    sz = tuple(int(x) for x in args.sizes.split(","))
+    reqs = serve.draw_requests(args.solves, rate=0.0, seed=7, end_time=(1.0, 1.0), degrees=dg, cells=sz)
     solves = [r.make_solve() for r in reqs]
     free, total = torch.cuda.mem_get_info()
     b = Batch(precision=args.precision, hbm_budget_bytes=int(free * 0.85), max_solves=len(solves) + 8)
@@ -470,8 +474,8 @@ def batch_workload(args, torch):
                          "frac": achieved / peak, "peak_source": "measured",
                          "kernel": "stage_cart_kernel (one launch per degree group and stage)"},
             "sequential_value": sequential, "batched_over_sequential": batched / sequential,
-            "config": {"workload": "batch of %d 3-D solves (k 3..7, n 8..32, Ricker, 8 receivers)"
-                                   % len(solves), "total_dofs": dofs, "precision": args.precision,
+            "config": {"workload": "batch of %d 3-D solves (k %d..%d, n %d..%d, Ricker, 8 receivers)"
+                                   % ((len(solves),) + dg + sz), "total_dofs": dofs, "precision": args.precision,
                        "sequential_sample": len(idx)}}
 
 

@@ -509,8 +509,7 @@ void split(double v, float* hi, float* lo) {
 
 bool cart_variant_in32(int cv) {
   return cv == ew::CV_MIX_APPLY32 || cv == ew::CV_MIX_MID || cv == ew::CV_MIX_LAST ||
-         cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF || cv == ew::CV_MIX_S1_FF ||
-         cv == ew::CV_MIX_LAST_BOTH;
+         cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF || cv == ew::CV_MIX_S1_FF;
 }
 bool cart_variant_apply(int cv) {
   return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32;

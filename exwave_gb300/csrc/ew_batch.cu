@@ -12,11 +12,12 @@
 // parity of the state double buffer; membership changes rebuild tables and
 // graphs before the next step.
 //
-// Mixed precision keeps each solve's FP64 state in U[0] and, between the
-// steps, also its split into FP32 hi (stage input buffer X[parity]) and lo
-// (U[1], as floats): the first stage of a step reads hi and lo like a
-// middle stage reads its input, and the last stage writes the FP64 state
-// together with its split.  Receivers and get_state read the FP64 state.
+// Mixed precision keeps each solve's state between the steps as an
+// unevaluated float pair: FP32 hi in the stage input buffer X[cur] and FP32
+// lo in U[1] (about 48 significant bits).  The first stage of a step reads
+// hi and lo like a middle stage reads its input, the accumulator lives in
+// U[0] during the step and the last stage writes the new hi and lo.
+// Receivers, get_state and set_state convert between the pair and FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -114,7 +115,10 @@ struct Solve {
 // Receiver sampling: one block per solve, one warp per receiver; then the
 // solve's clock advances by one step.
 struct RecDesc {
-  const double* U[2];
+  const double* U[2];  // FP64 state by parity (FP64 batches)
+  const float* H[2];   // mixed: hi part by parity
+  const float* L;      // mixed: lo part
+  int32_t mixed, pad;
   const double* rec_w;
   const int32_t* rec_cell;
   double* trace;
@@ -128,14 +132,16 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity) {
   if (s >= n) return;
   const RecDesc r = rd[s];
   const double* state = r.U[parity];
+  const float* hi = r.H[parity];
   const int64_t step = (int64_t)r.clock[1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int k = warp; k < r.n_rec; k += blockDim.x >> 5) {
     const int32_t cell = r.rec_cell[k];
-    const double* p = state + ((size_t)cell * r.F + r.dim) * r.N;
+    const size_t p0 = ((size_t)cell * r.F + r.dim) * r.N;
     const double* w = r.rec_w + (size_t)k * r.N;
     double acc = 0.0;
-    for (int q = lane; q < r.N; q += 32) acc += w[q] * p[q];
+    for (int q = lane; q < r.N; q += 32)
+      acc += w[q] * (r.mixed ? (double)hi[p0 + q] + (double)r.L[p0 + q] : state[p0 + q]);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) r.trace[step * r.n_rec + k] = acc;
   }
@@ -144,6 +150,13 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity) {
     r.clock[0] += r.dt;
     r.clock[1] = (double)(step + 1);
   }
+}
+
+// FP32 hi + lo -> FP64 state.
+__global__ void join_state_kernel(const float* hi, const float* lo, int64_t n, double* state) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    state[i] = (double)hi[i] + (double)lo[i];
 }
 
 // FP64 state -> FP32 hi and lo parts (hi + lo = state to about 48 bits).
@@ -318,18 +331,18 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
   const double* A[5];
   void* Xo[5];
   double* Ao[5];
-  float* Lo = nullptr;
   if (b->mixed) {
-    // state U[0]; hi in X[parity], lo in U[1] (floats)
+    // state pair: hi in X[parity], lo in U[1] (floats); accumulator in U[0];
+    // the last stage leaves the new hi in X[1 - parity] and lo in U[1]
     void* Xh = s.X[parity];
     void* Xn = s.X[1 - parity];
     double* S = s.U[0];
-    Lo = reinterpret_cast<float*>(s.U[1]);
-    X[0] = Xh; A[0] = reinterpret_cast<const double*>(Lo); Xo[0] = Xn; Ao[0] = S;
+    double* Lo = s.U[1];
+    X[0] = Xh; A[0] = Lo; Xo[0] = Xn; Ao[0] = S;
     X[1] = Xn; A[1] = S; Xo[1] = Xh; Ao[1] = S;
     X[2] = Xh; A[2] = S; Xo[2] = Xn; Ao[2] = S;
     X[3] = Xn; A[3] = S; Xo[3] = Xh; Ao[3] = S;
-    X[4] = Xh; A[4] = S; Xo[4] = Xn; Ao[4] = S;
+    X[4] = Xh; A[4] = S; Xo[4] = Xn; Ao[4] = Lo;
   } else {
     double* T = static_cast<double*>(s.X[0]);
     X[0] = Nv; A[0] = Nv; Xo[0] = T; Ao[0] = Pv;
@@ -345,7 +358,6 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
     d.A = A[st];
     d.Xout = Xo[st];
     d.Aout = Ao[st];
-    d.Lout = st == 4 ? Lo : nullptr;
     d.nbr = s.nbr;
     d.cellc = s.cellc;
     d.n_cells = s.n_cells;
@@ -393,7 +405,7 @@ int rebuild(ew_batch* b) {
     const int F = g.dim + 1;
     for (int st = 0; st < 5; ++st) {
       if (b->mixed) {
-        g.variant[st] = st == 0 ? ew::CV_MIX_S1_FF : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST_BOTH);
+        g.variant[st] = st == 0 ? ew::CV_MIX_S1_FF : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST_FF);
         g.sx[st] = 1;
       } else {
         g.variant[st] = st < 4 ? ew::CV_F64_MID : ew::CV_F64_LAST;
@@ -455,7 +467,12 @@ int rebuild(ew_batch* b) {
       const Solve& s = b->solves[id];
       RecDesc r;
       r.U[0] = s.U[0];
-      r.U[1] = b->mixed ? s.U[0] : s.U[1];  // mixed: the FP64 state stays in U[0]
+      r.U[1] = s.U[1];
+      r.H[0] = static_cast<const float*>(s.X[0]);
+      r.H[1] = static_cast<const float*>(s.X[1]);
+      r.L = reinterpret_cast<const float*>(s.U[1]);
+      r.mixed = b->mixed ? 1 : 0;
+      r.pad = 0;
       r.rec_w = s.rec_w;
       r.rec_cell = s.rec_cell;
       r.trace = s.trace;
@@ -731,7 +748,6 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   // mixed: the zero state's hi and lo parts
   for (int k = 0; b->mixed && k < 2; ++k)
     if (e == cudaSuccess) e = cudaMemsetAsync(s.X[k], 0, (size_t)s.n_dofs * 4, b->stream);
-  if (b->mixed) s.cur = 0;
   if (e == cudaSuccess) e = cudaMemsetAsync(s.clock, 0, 16, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // host vectors go out of scope
   if (e != cudaSuccess) {
@@ -762,15 +778,17 @@ int ew_batch_set_state(ew_batch* b, int32_t id, const double* state) {
   if (!s) return bfail(b, EW_ERR_INVALID, "unknown solve id");
   cudaSetDevice(b->device);
   if (s->steps_done != 0) return bfail(b, EW_ERR_INVALID, "set_state before the first step only");
-  cudaError_t e = cudaMemcpyAsync(s->U[s->cur], state, (size_t)s->n_dofs * 8,
-                                  cudaMemcpyDeviceToDevice, b->stream);
-  if (e == cudaSuccess && b->mixed) {
-    // hi and lo parts for the next first stage
+  cudaError_t e;
+  if (b->mixed) {
+    // the state's hi and lo parts, read by the next first stage
     const int threads = 256;
     const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
     split_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
-        s->U[0], s->n_dofs, static_cast<float*>(s->X[b->parity]), reinterpret_cast<float*>(s->U[1]));
+        state, s->n_dofs, static_cast<float*>(s->X[s->cur]), reinterpret_cast<float*>(s->U[1]));
     e = cudaGetLastError();
+  } else {
+    e = cudaMemcpyAsync(s->U[s->cur], state, (size_t)s->n_dofs * 8, cudaMemcpyDeviceToDevice,
+                        b->stream);
   }
   return e == cudaSuccess ? EW_OK : bcuda(b, e, "set state");
 }
@@ -780,8 +798,18 @@ int ew_batch_get_state(ew_batch* b, int32_t id, double* state) {
   Solve* s = find(b, id);
   if (!s) return bfail(b, EW_ERR_INVALID, "unknown solve id");
   cudaSetDevice(b->device);
-  cudaError_t e = cudaMemcpyAsync(state, s->U[s->cur], (size_t)s->n_dofs * 8,
-                                  cudaMemcpyDeviceToDevice, b->stream);
+  cudaError_t e;
+  if (b->mixed) {
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
+    join_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
+        static_cast<const float*>(s->X[s->cur]), reinterpret_cast<const float*>(s->U[1]), s->n_dofs,
+        state);
+    e = cudaGetLastError();
+  } else {
+    e = cudaMemcpyAsync(state, s->U[s->cur], (size_t)s->n_dofs * 8, cudaMemcpyDeviceToDevice,
+                        b->stream);
+  }
   return e == cudaSuccess ? EW_OK : bcuda(b, e, "get state");
 }
 
@@ -816,7 +844,7 @@ int ew_batch_step(ew_batch* b, int32_t n_steps) {
   for (auto& kv : b->solves)
     if (kv.second.steps_done < kv.second.n_steps) {
       kv.second.steps_done += n_steps;
-      if (!b->mixed) kv.second.cur ^= (n_steps & 1);
+      kv.second.cur ^= (n_steps & 1);
       if (kv.second.steps_done >= kv.second.n_steps) finished = true;
     }
   // parity changed for everyone: solves keep their state in U[parity]

@@ -254,9 +254,6 @@ struct CartSmem {
 //                place of A)
 //  MIX_LAST_FF : last stage of such a step: the new state is left as that
 //                pair, hi to Xout and lo to Aout (no rounding to FP64)
-//  MIX_LAST_BOTH: last stage of a batched step: the new state goes out as
-//                FP64 (Aout) and as the pair hi (Xout) / lo (Lout) that the
-//                next step's MIX_S1_FF reads
 // Within an LSRK step the mixed path keeps the accumulator as an unevaluated
 // sum hi + lo of two floats (about 48 significant bits) in the 8-byte slot
 // of the FP64 vector, updated with error-free transformations on the FP32
@@ -270,22 +267,18 @@ enum Epi : int {
   EPI_MIX_LAST = 5,
   EPI_MIX_UPD = 6,
   EPI_MIX_S1_FF = 7,
-  EPI_MIX_LAST_FF = 8,
-  EPI_MIX_LAST_BOTH = 9
+  EPI_MIX_LAST_FF = 8
 };
 
 template <int EPI>
 struct EpiTraits {
   static constexpr bool stage_a = EPI != EPI_APPLY;
   static constexpr bool writes_x = EPI == EPI_F64_MID || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID ||
-                                   EPI == EPI_MIX_S1_FF || EPI == EPI_MIX_LAST_FF ||
-                                   EPI == EPI_MIX_LAST_BOTH;
+                                   EPI == EPI_MIX_S1_FF || EPI == EPI_MIX_LAST_FF;
   // A is the FP32 lo array of a float-pair state whose hi array is X
   static constexpr bool lo_in = EPI == EPI_MIX_S1_FF;
   // the new state is written as hi (Xout) and lo (Aout, FP32) arrays
   static constexpr bool lo_out = EPI == EPI_MIX_LAST_FF;
-  // FP64 state to Aout, its hi part to Xout and lo part to Lout
-  static constexpr bool both_out = EPI == EPI_MIX_LAST_BOTH;
   static constexpr int a_elem = lo_in ? 4 : 8;
 };
 
@@ -343,12 +336,6 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
     xn = static_cast<OutT>(rh);
     an = ff_pack(rh, rl);
-  } else if constexpr (EPI == EPI_MIX_LAST_BOTH) {
-    // the pair is returned: the store writes its FP64 sum, hi and lo
-    float rh, rl;
-    ff_add(ff_hi(a), ff_lo(a), fmaf(sd.f1_hi, k, sd.f1_lo * k), rh, rl);
-    xn = static_cast<OutT>(rh);
-    an = ff_pack(rh, rl);
   } else {  // EPI_MIX_UPD
     an = a + f32_to_f64(fmaf(sd.f1_hi, k, sd.f1_lo * k));
   }
@@ -379,7 +366,6 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
   constexpr bool CONV = sizeof(Real) == 4 && sizeof(InT) == 8;
   constexpr bool LO_IN = EpiTraits<EPI>::lo_in;
   constexpr bool LO_OUT = EpiTraits<EPI>::lo_out;
-  constexpr bool BOTH_OUT = EpiTraits<EPI>::both_out;
   constexpr int A_ELEM = EpiTraits<EPI>::a_elem;
   const LaunchArgs& La = ca.la;
   const int CB = La.cells_per_block;
@@ -510,10 +496,6 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
       if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
       if constexpr (LO_OUT) {
         reinterpret_cast<float*>(sd.Aout)[g] = ff_lo(an);
-      } else if constexpr (BOTH_OUT) {
-        // an holds the pair (hi, lo): FP64 value and the lo part
-        sd.Aout[g] = f32_to_f64(ff_hi(an)) + f32_to_f64(ff_lo(an));
-        sd.Lout[g] = ff_lo(an);
       } else {
         sd.Aout[g] = an;
       }
@@ -728,7 +710,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
             double a0, a1 = 0.0;
             epi_value<EPI, Real, OutT>(sd, aval(l0 + i * str), ku[i], x0, a0);
             if (i + 1 < NP) epi_value<EPI, Real, OutT>(sd, aval(l0 + (i + 1) * str), ku[i + 1], x1, a1);
-            if (paired && !BOTH_OUT) {
+            if (paired) {
               if constexpr (EpiTraits<EPI>::writes_x) store2(static_cast<OutT*>(sd.Xout) + g0 + i, x0, x1);
               if constexpr (LO_OUT)
                 store2(reinterpret_cast<float*>(sd.Aout) + g0 + i, ff_lo(a0), ff_lo(a1));

@@ -66,9 +66,6 @@ struct SolveDesc {
   double src_amp, src_f0, src_t0, c_stage, dt;
   int32_t src_cell;    // -1: none
   int32_t pad2;
-  // MIX_LAST_BOTH: FP32 lo part of the new state ([cell][field][point]);
-  // its hi part goes to Xout
-  float* Lout;
 };
 
 // Ricker wavelet (1 - 2 pi^2 f0^2 s^2) exp(-pi^2 f0^2 s^2), s = t - t0.

@@ -167,7 +167,6 @@ void EW_TABLE_FN(KernelTable& t) {
   fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
   fill_cart<CartK<float, float, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
   fill_cart<CartK<float, float, EPI_MIX_LAST_FF>>(t.cart[CV_MIX_LAST_FF]);
-  fill_cart<CartK<float, float, EPI_MIX_LAST_BOTH>>(t.cart[CV_MIX_LAST_BOTH]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);

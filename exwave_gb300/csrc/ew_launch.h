@@ -36,8 +36,7 @@ enum CartVariant : int {
   CV_MIX_UPD = 8,     // mixed ADER update u + M^-1 A(T)
   CV_MIX_S1_FF = 9,   // mixed stage 1, state held as float pairs (multi-step calls)
   CV_MIX_LAST_FF = 10,  // mixed stage 5, state left as float pairs
-  CV_MIX_LAST_BOTH = 11,  // mixed stage 5, FP64 state and its float pair out (batches)
-  N_CART_VARIANTS = 12
+  N_CART_VARIANTS = 11
 };
 
 // Launcher of the Cartesian line kernel.
