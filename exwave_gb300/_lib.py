@@ -27,7 +27,7 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_receivers",
            "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches",
            "ew_tune_set", "ew_tune_get", "ew_lsrk45_step_static", "ew_lsrk45_steps",
-           "ew_set_receivers", "ew_sample_receivers"]
+           "ew_set_receivers", "ew_sample_receivers", "ew_aderadconfull_step"]
 
 
 class EwError(RuntimeError):
@@ -84,6 +84,7 @@ def load():
         "ew_lsrk45_step_static": (ctypes.c_int, [vp, d, dp, dp]),
         "ew_lsrk45_steps": (ctypes.c_int, [vp, d, i64, dp, dp]),
         "ew_set_receivers": (ctypes.c_int, [vp, i32, dp]),
+        "ew_aderadconfull_step": (ctypes.c_int, [vp, d, dp, dp]),
         "ew_sample_receivers": (ctypes.c_int, [vp, dp, dp]),
         "ew_apply_ader": (ctypes.c_int, [vp, d, dp, dp]),
         "ew_ader_step": (ctypes.c_int, [vp, d, dp, dp]),

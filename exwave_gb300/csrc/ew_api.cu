@@ -82,6 +82,13 @@ struct Modes {
 };
 
 // ---------------------------------------------------------------- kernels
+// y += c x
+__global__ void axpy_kernel(int64_t n, double c, const double* x, double* y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += c * x[i];
+}
+
 __global__ void rk_update_kernel(int64_t n, double f1, double f2, int is_last, const double* v1,
                                  double* v2, double* v3) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -330,6 +337,8 @@ struct ew_ctx {
   int32_t n_rec = 0;
   int32_t* d_rec_cell = nullptr;
   double* d_rec_w = nullptr;
+  // ADERADCONFULL: two FP64 vectors for the repeated operator applications
+  double* d_ad[2] = {nullptr, nullptr};
   std::string last_error;
   int64_t launches = 0;
 };
@@ -373,7 +382,7 @@ void free_ctx(ew_ctx* c) {
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
                   c->d_work_stage, c->d_work_ck, c->d_work_cart, c->d_cellc, c->d_err, c->d_tmp64, c->d_x32[0],
-                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w};
+                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w, c->d_ad[0], c->d_ad[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -1108,6 +1117,40 @@ int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst) {
   const int var = ctx->mixed ? ew::STAGE_MIX_IN32 : ew::STAGE_F64;
   const int cv = ctx->mixed ? ew::CV_MIX_APPLY32 : ew::CV_F64_APPLY;
   return launch_stage(ctx, var, cv, nullptr, T, nullptr, dst, ew::MODE_APPLY, 0.0, 0.0, -1.0f);
+}
+
+int ew_aderadconfull_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_aderadconfull_step: vec_n and vec_np must be distinct");
+  // w_0 = u, w_{j+1} = M^-1 A(w_j); u' = u + dt w_1 + sum_{j=1..k} fac_j (-1)^j w_{j+1}
+  // with fac_1 = -dt^2/2, fac_{j+1} = -fac_j dt / (j + 2): the reference's
+  // series (its intermediate vectors are -(previous result)), signs folded
+  // into the coefficients
+  for (int i = 0; i < 2; ++i)
+    if (!ctx->d_ad[i] && (rc = dev_alloc(ctx, &ctx->d_ad[i], (size_t)ctx->n_dofs))) return rc;
+  cudaError_t e = cudaMemcpyAsync(vec_np, vec_n, (size_t)ctx->n_dofs * 8, cudaMemcpyDeviceToDevice,
+                                  ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "copy");
+  const int var = ctx->mixed ? ew::STAGE_MIX_IN64 : ew::STAGE_F64;
+  const int cv = ctx->mixed ? ew::CV_MIX_APPLY64 : ew::CV_F64_APPLY;
+  double fac = -0.5 * dt * dt;
+  for (int j = 0; j <= ctx->degree; ++j) {
+    const double* in = j == 0 ? vec_n : ctx->d_ad[(j - 1) & 1];
+    double* out = ctx->d_ad[j & 1];
+    if ((rc = launch_stage(ctx, var, cv, nullptr, in, nullptr, out, ew::MODE_APPLY, 0.0, 0.0, 1.0f)))
+      return rc;
+    double c = dt;
+    if (j > 0) {
+      c = (j & 1) ? -fac : fac;
+      fac *= -dt / (j + 2);
+    }
+    ew::axpy_kernel<<<ew::grid_for(ctx->n_dofs), 256, 0, ctx->stream>>>(ctx->n_dofs, c, out, vec_np);
+    ++ctx->launches;
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "axpy launch");
+  }
+  return EW_OK;
 }
 
 int ew_ader_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np) {

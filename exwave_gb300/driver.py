@@ -3,10 +3,11 @@
 output of L2 errors at every tick."""
 from . import mesh as mesh_mod
 from .operator import WaveEquationOperation, reference_mode
-from .time_integrators import ArbitraryHighOrderDG, ClassRK4, LowStorageRK45Reg2
+from .time_integrators import AderAdconFull, ArbitraryHighOrderDG, ClassRK4, LowStorageRK45Reg2
 from .utilities import TimeControl
 
-SUPPORTED = {"LSRK45R2": LowStorageRK45Reg2, "clRK4": ClassRK4, "ADER": ArbitraryHighOrderDG}
+SUPPORTED = {"LSRK45R2": LowStorageRK45Reg2, "clRK4": ClassRK4, "ADER": ArbitraryHighOrderDG,
+             "ADERADCONFULL": AderAdconFull}
 
 
 def run(params, precision="fp64", on_output=None):

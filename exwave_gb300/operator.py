@@ -123,6 +123,9 @@ class WaveEquationOperation:
         self._chk(self.L.ew_sample_receivers(self.ctx, _ptr(state), _ptr(out)))
         return out.view(self.n_receivers, self.dim + 1)
 
+    def aderadconfull_step(self, dt, vec_n, vec_np):
+        self._chk(self.L.ew_aderadconfull_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
+
     def ader_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_ader_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 

@@ -24,6 +24,15 @@ class ArbitraryHighOrderDG(ExplicitIntegrator):
         op.ader_step(time_step, vec_n, vec_np)
 
 
+class AderAdconFull(ExplicitIntegrator):
+    """The ADER step with the operator of WaveEquationOperationADERADCONFULL
+    (wave_equation_operations.cc:689-735): the Taylor series of the time
+    integral from k+1 applications of the full DG operator."""
+
+    def perform_time_step(self, vec_n, vec_np, time_step, op):
+        op.aderadconfull_step(time_step, vec_n, vec_np)
+
+
 class ClassRK4(ExplicitIntegrator):
     """Classical RK4 (time_integrators.cc:66-102) composed from apply and
     vector updates."""

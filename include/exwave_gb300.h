@@ -135,6 +135,13 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
  * earlier set. */
 int ew_set_receivers(ew_ctx* ctx, int32_t n, const double* points);
 
+/* ADER in its ADERADCONFULL form: WaveEquationOperationADERADCONFULL::apply_ader
+ * (wave_equation_operations.cc:689-735), the Taylor series of the time
+ * integral built from k+1 applications of the full DG operator, followed by
+ * the update of ArbitraryHighOrderDG::perform_time_step (time_integrators.cc:37-50).
+ * vec_n is not modified; two FP64 work vectors are allocated on first use. */
+int ew_aderadconfull_step(ew_ctx* ctx, double dt, const double* vec_n, double* vec_np);
+
 /* Every field (u_0..u_{d-1}, p) of a device state at the receivers into the
  * device array out (n x (dim+1), receiver-major), on the context's stream. */
 int ew_sample_receivers(ew_ctx* ctx, const double* state, double* out);

@@ -13,7 +13,7 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_runs.json"
 with open(GOLDEN) as f:
     RUNS = json.load(f)
 NAMES = ["lsrk45r2_2d_cartesian", "clrk4_3d", "ader_2d_norecon_ref2", "ader_2d_recon_ref2",
-         "ader_2d_recon_ref3", "ader_3d_norecon"]
+         "ader_2d_recon_ref3", "ader_3d_norecon", "aderadconfull_2d"]
 
 
 @pytest.mark.parametrize("name", NAMES)
