@@ -464,6 +464,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
 
   uint32_t phase = 0;  // bit b: parity of the next wait on buffer b
   int it = 0;
+  bool prev_a_ok = true;  // the previous item's accumulator copy arrived
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
     const int b = it & 1;
     const bool has_next = w + (int)gridDim.x < La.n_work;
@@ -485,12 +486,6 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
         return sA[idx];
       }
     };
-    // the single A buffer was last read before the previous end-of-item
-    // barrier: refill it now, it is needed only by the epilogue
-    if (ca.tma && a_single && threadIdx.x == 0) {
-      fence_proxy_async();
-      issue_a(wi);
-    }
     // one value's outputs: next stage input and accumulator / new state
     auto store_out = [&](size_t g, OutT xn, double an) {
       if constexpr (EpiTraits<EPI>::writes_x) static_cast<OutT*>(sd.Xout)[g] = xn;
@@ -517,26 +512,32 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
     // wait and the own-line contractions, awaited just before the fluxes
     prefetch_nb(wi, sd, nbs);
     if (ca.tma) {
-      // prefetch the next item into the other buffer (its previous contents
-      // were consumed before the end-of-item barrier of the last iteration)
-      if (threadIdx.x == 0 && has_next) {
-        fence_proxy_async();
-        issue(La.work[w + gridDim.x], b ^ 1);
-      }
       const bool ok = mbar_wait(&bars[b], (phase >> b) & 1u);
       phase ^= (1u << b);
-      if (__syncthreads_or(!ok)) {
+      // One barrier both ends the previous item (its pressure phase read the
+      // accumulator buffer and, for float-pair input, the other X buffer)
+      // and starts this one (cell constants written, X landed).
+      if (__syncthreads_or(!ok || !prev_a_ok)) {
         // give up on this CTA's remaining items: wait (bounded) for the
         // copies still in flight, then leave
         if (threadIdx.x == 0) {
           atomicOr(La.err, ERR_WAIT_TIMEOUT);
-          if (has_next) mbar_wait(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-          if (a_single) mbar_wait(&bars[2], (uint32_t)it & 1u);
+          if (!ok) mbar_wait(&bars[b], ((phase >> b) & 1u) ^ 1u);
+          if (a_single && it > 0) mbar_wait(&bars[2], (uint32_t)(it - 1) & 1u);
         }
         cp_async_wait_all();
+        prev_a_ok = true;
         break;
       }
+      if (threadIdx.x == 0) {
+        fence_proxy_async();
+        // the next item into the other buffer, and this item's accumulator
+        // (single buffer, needed only by the epilogue)
+        if (has_next) issue(La.work[w + gridDim.x], b ^ 1);
+        if (a_single) issue_a(wi);
+      }
     } else {
+      __syncthreads();  // the previous item is done with the buffers
       const size_t c0 = (size_t)wi.cell_begin * F * N;
       if (stage_x) {
         const InT* gx = static_cast<const InT*>(sd.X) + c0;
@@ -549,8 +550,8 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
         const double* ga = sd.A + c0;
         for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sA[i] = ga[i];
       }
+      __syncthreads();
     }
-    __syncthreads();
     if constexpr (CONV) {
       // FP32 operator on FP64 values: each staged value is converted once,
       // in place, to a float pair (hi in the low word is the operator input).
@@ -745,15 +746,14 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
       epi_value<EPI, Real, OutT>(sd, aval(lidx), k, xn, an);
       store_out(g, xn, an);
     }
-    if (__syncthreads_or(!a_ok)) {
-      // the accumulator copy timed out: stop as on an X time-out
-      if (threadIdx.x == 0) {
-        atomicOr(La.err, ERR_WAIT_TIMEOUT);
-        if (has_next) mbar_wait(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-        mbar_wait(&bars[2], (uint32_t)it & 1u);
-      }
-      cp_async_wait_all();
-      break;
+    // no end-of-item barrier: the next item's first barrier ends this one
+    prev_a_ok = a_ok;
+  }
+  // the last item's copies: none may be in flight when the block ends
+  if (__syncthreads_or(!prev_a_ok)) {
+    if (threadIdx.x == 0) {
+      atomicOr(La.err, ERR_WAIT_TIMEOUT);
+      mbar_wait(&bars[2], (uint32_t)(it - 1) & 1u);
     }
   }
 }
