@@ -767,6 +767,202 @@ void l2_errors(const Oracle& O, const double* sol, Exact exact, double* out) {
   out[2] = std::sqrt(mag);
 }
 
+// WaveEquationOperation::compute_post_pressure (wave_equation_operations.cc:784-848)
+// and the "error p post" of output_results (explicit_wave.cc:476-484): on
+// every cell the Q_{k+1} pressure p* with (grad phi, grad p*) =
+// (grad phi, -rho du/dt) for all phi in Q_{k+1} (QGauss(k+2) on the mapped
+// cell; du/dt is the velocity part of M^-1 A(u)), solved with the
+// reference's unpreconditioned CG (first unknown constrained, relative
+// tolerance 1e-11), shifted to the mean of p, and its L2 error against the
+// exact pressure with QGauss(k+3).  p* is written by its values at the
+// QGauss(k+2) points (any basis of Q_{k+1} gives the same function).
+template <class Exact>
+double post_pressure_error(Oracle& O, const double* sol, Exact exact) {
+  const int dim = O.dim, n = O.n, F = O.F, N = O.N;
+  std::vector<double> tmp((size_t)O.n_dofs());
+  O.apply(sol, tmp.data());
+  const int m = n + 1, Mp = ipow(m, dim);
+  Basis1D P(m);                    // Lagrange basis at the QGauss(k+2) points
+  std::vector<double> I(m * n);    // Q_k values at n Gauss points -> m points
+  for (int a = 0; a < m; ++a)
+    for (int i = 0; i < n; ++i) I[a * n + i] = O.B.lag.value(i, P.rule.x[a]);
+  const Rule er = gauss_rule(m + 1);  // QGauss(k+3)
+  const int me = er.n, Me = ipow(me, dim);
+  std::vector<double> Ie(me * m);
+  for (int a = 0; a < me; ++a)
+    for (int i = 0; i < m; ++i) Ie[a * m + i] = P.lag.value(i, er.x[a]);
+  const double ABS_TOL = 1e-20, REL_TOL = 1e-11;
+  double esum = 0.0;
+#pragma omp parallel reduction(+ : esum)
+  {
+    std::vector<double> cellv, vq, pq, jxw(Mp), met(Mp * 9), rhs(Mp), x(Mp), r(Mp), pv(Mp), v(Mp),
+        g(3 * Mp), xe;
+    // y = K x: the Laplacian (grad phi_i, grad phi_j) with unknown 0 constrained
+    auto lap = [&](const std::vector<double>& in, std::vector<double>& out) {
+      std::vector<double> z(in);
+      z[0] = 0.0;
+      for (int q = 0; q < Mp; ++q) {
+        int ii[3] = {0, 0, 0}, t = q, str[3] = {1, m, m * m};
+        for (int e = 0; e < dim; ++e) {
+          ii[e] = t % m;
+          t /= m;
+        }
+        double gr[3] = {0, 0, 0};
+        for (int e = 0; e < dim; ++e)
+          for (int a = 0; a < m; ++a) gr[e] += P.D[ii[e] * m + a] * z[q + (a - ii[e]) * str[e]];
+        for (int e = 0; e < dim; ++e) {
+          double s = 0.0;
+          for (int f = 0; f < dim; ++f) s += met[q * 9 + e * 3 + f] * gr[f];
+          g[e * Mp + q] = jxw[q] * s;
+        }
+      }
+      for (int i = 0; i < Mp; ++i) {
+        int ii[3] = {0, 0, 0}, t = i, str[3] = {1, m, m * m};
+        for (int e = 0; e < dim; ++e) {
+          ii[e] = t % m;
+          t /= m;
+        }
+        double s = 0.0;
+        for (int e = 0; e < dim; ++e)
+          for (int a = 0; a < m; ++a) s += P.D[a * m + ii[e]] * g[e * Mp + i + (a - ii[e]) * str[e]];
+        out[i] = s;
+      }
+      out[0] = in[0];
+    };
+    auto dot = [&](const std::vector<double>& a, const std::vector<double>& b) {
+      double s = 0.0;
+      for (int i = 0; i < Mp; ++i) s += a[i] * b[i];
+      return s;
+    };
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t c = 0; c < O.mesh.n_cells; ++c) {
+      const double* V = &O.mesh.vert[(size_t)c * (1 << dim) * dim];
+      const double rho = O.mesh.density[c];
+      cellv.assign(tmp.begin() + (size_t)c * F * N, tmp.begin() + (size_t)(c + 1) * F * N);
+      O.tensor_apply(I, m, n, cellv, vq);  // du/dt at the m^dim points (fields 0..dim-1)
+      cellv.assign(sol + (size_t)c * F * N, sol + (size_t)(c + 1) * F * N);
+      O.tensor_apply(I, m, n, cellv, pq);  // p at the m^dim points (field dim)
+      double vol = 0.0, pint = 0.0;
+      for (int q = 0; q < Mp; ++q) {
+        int t = q;
+        double xi[3] = {0, 0, 0}, w = 1.0;
+        for (int e = 0; e < dim; ++e) {
+          xi[e] = P.rule.x[t % m];
+          w *= P.rule.w[t % m];
+          t /= m;
+        }
+        double J[3][3], JiT[3][3];
+        jacobian(dim, V, xi, J);
+        jxw[q] = std::fabs(inverse_transpose(dim, J, JiT)) * w;
+        for (int e = 0; e < dim; ++e)
+          for (int f = 0; f < dim; ++f) {
+            double s = 0.0;
+            for (int d = 0; d < dim; ++d) s += JiT[d][e] * JiT[d][f];
+            met[q * 9 + e * 3 + f] = s;
+          }
+        // reference-coordinate flux of -rho du/dt: sum_d JiT[d][e] (-rho v_d)
+        for (int e = 0; e < dim; ++e) {
+          double s = 0.0;
+          for (int d = 0; d < dim; ++d) s += JiT[d][e] * (-rho * vq[d * Mp + q]);
+          g[e * Mp + q] = jxw[q] * s;
+        }
+        vol += jxw[q];
+        pint += jxw[q] * pq[dim * Mp + q];
+      }
+      for (int i = 0; i < Mp; ++i) {
+        int ii[3] = {0, 0, 0}, t = i, str[3] = {1, m, m * m};
+        for (int e = 0; e < dim; ++e) {
+          ii[e] = t % m;
+          t /= m;
+        }
+        double s = 0.0;
+        for (int e = 0; e < dim; ++e)
+          for (int a = 0; a < m; ++a) s += P.D[a * m + ii[e]] * g[e * Mp + i + (a - ii[e]) * str[e]];
+        rhs[i] = s;
+      }
+      rhs[0] = 0.0;
+      // SolverCGvect::solve (elementwise_cg.templates.h:64-145), identity preconditioner
+      std::fill(x.begin(), x.end(), 0.0);
+      r = rhs;
+      const double r0 = std::sqrt(dot(r, r));
+      if (r0 > 0.0) {
+        pv = r;
+        double ry = dot(r, pv);
+        for (int it = 1; it <= 6 * Mp; ++it) {
+          lap(pv, v);
+          double pvv = dot(pv, v);
+          if (std::fabs(pvv) < ABS_TOL) pvv = ABS_TOL;
+          const double alpha = ry / pvv;
+          for (int i = 0; i < Mp; ++i) {
+            x[i] += alpha * pv[i];
+            r[i] -= alpha * v[i];
+          }
+          const double rn = std::sqrt(dot(r, r));
+          if (rn < ABS_TOL || rn / r0 < REL_TOL) break;
+          const double ry_new = dot(r, r);
+          const double beta = ry_new / ry;
+          for (int i = 0; i < Mp; ++i) pv[i] = r[i] + beta * pv[i];
+          ry = ry_new;
+        }
+      }
+      // mean of p
+      double sint = 0.0;
+      for (int q = 0; q < Mp; ++q) sint += jxw[q] * x[q];
+      const double shift = (pint - sint) / vol;
+      for (int q = 0; q < Mp; ++q) x[q] += shift;
+      // error with QGauss(k+3)
+      xe.assign(Me, 0.0);
+      {
+        // tensor interpolation of the single field x from m to me points
+        std::vector<double> cur(x), nxt;
+        int ext[3] = {m, m, m};
+        for (int e = 0; e < dim; ++e) {
+          int sz_out = 1;
+          for (int f = 0; f < dim; ++f) sz_out *= (f == e ? me : ext[f]);
+          nxt.assign(sz_out, 0.0);
+          const int s0 = (e == 0) ? 1 : (e == 1 ? ext[0] : ext[0] * ext[1]);
+          for (int o = 0; o < sz_out; ++o) {
+            int idx[3] = {0, 0, 0}, t = o;
+            for (int f = 0; f < dim; ++f) {
+              const int ef = (f == e) ? me : ext[f];
+              idx[f] = t % ef;
+              t /= ef;
+            }
+            int base = 0, mul = 1;
+            for (int f = 0; f < dim; ++f) {
+              base += (f == e ? 0 : idx[f]) * mul;
+              mul *= ext[f];
+            }
+            double s = 0.0;
+            for (int a = 0; a < m; ++a) s += Ie[idx[e] * m + a] * cur[base + a * s0];
+            nxt[o] = s;
+          }
+          cur.swap(nxt);
+          ext[e] = me;
+        }
+        xe = cur;
+      }
+      for (int q = 0; q < Me; ++q) {
+        int t = q;
+        double xi[3] = {0, 0, 0}, w = 1.0;
+        for (int e = 0; e < dim; ++e) {
+          xi[e] = er.x[t % me];
+          w *= er.w[t % me];
+          t /= me;
+        }
+        double J[3][3], JiT[3][3], xp[3] = {0, 0, 0}, ex[4];
+        jacobian(dim, V, xi, J);
+        const double jw = std::fabs(inverse_transpose(dim, J, JiT)) * w;
+        map_point(dim, V, xi, xp);
+        exact(xp, ex);
+        const double d = xe[q] - ex[dim];
+        esum += d * d * jw;
+      }
+    }
+  }
+  return std::sqrt(esum);
+}
+
 thread_local std::string g_last_error;
 
 }  // namespace
@@ -997,6 +1193,13 @@ void ewo_aderadconfull_step(ewo_problem* p, double dt, const double* vec_n, doub
   for (int64_t i = 0; i < nd; ++i) vec_np[i] = -acc[i] + vec_n[i];
 }
 
+// "error p post" against the reference's single-mode solution.
+double ewo_post_error_reference(ewo_problem* p, const double* u, int modes, double t) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  const int dim = O->dim;
+  return post_pressure_error(*O, u, [&](const double* x, double* ex) { exact_reference(dim, modes, x, t, ex); });
+}
+
 // L2 errors against the reference's single-mode solution: out = {err p, err u, |p|}.
 void ewo_errors_reference(ewo_problem* p, const double* u, int modes, double t, double* out) {
   Oracle* O = reinterpret_cast<Oracle*>(p);
@@ -1037,12 +1240,13 @@ int ewo_run_reference(ewo_problem* p, int integrator, double cfl, double final_t
     if (nrows >= max_rows) return;
     double e[3];
     ewo_errors_reference(p, sol.data(), modes, time, e);
-    double* r = rows + 5 * nrows;
+    double* r = rows + 6 * nrows;
     r[0] = time;
     r[1] = step;
     r[2] = e[0];
     r[3] = e[1];
     r[4] = e[2];
+    r[5] = ewo_post_error_reference(p, sol.data(), modes, time);
     ++nrows;
   };
   emit();

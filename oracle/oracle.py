@@ -70,6 +70,8 @@ def lib():
         L.ewo_run_reference.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, dp,
                                         ctypes.c_int, dp]
+        L.ewo_post_error_reference.restype = ctypes.c_double
+        L.ewo_post_error_reference.argtypes = [P, dp, ctypes.c_int, ctypes.c_double]
         L.ewo_point_values.restype = ctypes.c_int
         L.ewo_point_values.argtypes = [P, dp, ctypes.c_int, dp, dp]
         L.ewo_lsrk45_step_source.restype = ctypes.c_int
@@ -190,6 +192,9 @@ class Problem:
         lib().ewo_errors_reference(self.h, _dp(np.ascontiguousarray(u)), modes, t, _dp(out))
         return out
 
+    def post_error_reference(self, u, modes, t):
+        return lib().ewo_post_error_reference(self.h, _dp(np.ascontiguousarray(u)), modes, t)
+
     def errors_modes(self, u, amps, kvecs, t):
         amps = np.ascontiguousarray(amps, dtype=np.float64)
         kv = np.zeros((len(amps), 3), dtype=np.int32)
@@ -215,7 +220,7 @@ class Problem:
             raise RuntimeError(lib().ewo_last_error().decode())
 
     def run_reference(self, integrator, cfl, final_time, tick, modes, max_time_steps=1000000):
-        rows = np.zeros((4096, 5))
+        rows = np.zeros((4096, 6))  # time, step, err p, err v, |p|, err p post
         dt = np.zeros(1)
         nr = lib().ewo_run_reference(self.h, INTEGRATORS[integrator], cfl, final_time, tick, modes,
                                      max_time_steps, _dp(rows), rows.shape[0], _dp(dt))
