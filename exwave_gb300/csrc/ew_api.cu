@@ -293,6 +293,235 @@ __global__ void l2_kernel(const double* verts, int64_t n_cells, int dim, int np,
   }
 }
 
+// inverse transpose of the multilinear map's Jacobian (FP64): returns det J,
+// JiT[d][e] = d xi_e / d x_d
+__device__ double jac_inv_t_dev(int dim, const double* V, const double* xi, double JiT[3][3]) {
+  const int nv = 1 << dim;
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int v = 0; v < nv; ++v)
+    for (int j = 0; j < dim; ++j) {
+      double dphi = ((v >> j) & 1) ? 1.0 : -1.0;
+      for (int e = 0; e < dim; ++e)
+        if (e != j) dphi *= ((v >> e) & 1) ? xi[e] : 1.0 - xi[e];
+      for (int i = 0; i < dim; ++i) J[i][j] += V[v * dim + i] * dphi;
+    }
+  if (dim == 2) {
+    const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    JiT[0][0] = J[1][1] / det;
+    JiT[0][1] = -J[1][0] / det;
+    JiT[1][0] = -J[0][1] / det;
+    JiT[1][1] = J[0][0] / det;
+    return det;
+  }
+  const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1], c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2],
+               c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0], c10 = J[0][2] * J[2][1] - J[0][1] * J[2][2],
+               c11 = J[0][0] * J[2][2] - J[0][2] * J[2][0], c12 = J[0][1] * J[2][0] - J[0][0] * J[2][1],
+               c20 = J[0][1] * J[1][2] - J[0][2] * J[1][1], c21 = J[0][2] * J[1][0] - J[0][0] * J[1][2],
+               c22 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  JiT[0][0] = c00 / det; JiT[0][1] = c01 / det; JiT[0][2] = c02 / det;
+  JiT[1][0] = c10 / det; JiT[1][1] = c11 / det; JiT[1][2] = c12 / det;
+  JiT[2][0] = c20 / det; JiT[2][1] = c21 / det; JiT[2][2] = c22 / det;
+  return det;
+}
+
+// sum over the block, returned to every thread (red: 33 doubles)
+__device__ double block_sum_all(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) s += red[i];
+    red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// Post-processed pressure (WaveEquationOperation::compute_post_pressure,
+// wave_equation_operations.cc:784-848) and its L2 error against the
+// membrane solution (explicit_wave.cc:476-484).  One block per cell, one
+// thread per point of QGauss(k+2) (m = k+2 per direction, Mp = m^dim): the
+// Q_{k+1} pressure p* held by its values there solves
+// (grad phi, grad p*) = (grad phi, -rho du/dt) with the reference's
+// unpreconditioned CG (first unknown constrained, relative tolerance 1e-11,
+// at most 6 Mp iterations), is shifted to the mean of p and compared with
+// the exact pressure by QGauss(k+3).  Basis data in `pb`: interp (m x np),
+// qx (m), qw (m), D (m x m, derivative of the Lagrange basis at qx),
+// Ie ((m+1) x m, to the QGauss(k+3) points), ex (m+1), ew (m+1).  The block
+// is Mp rounded up to whole warps; the padding threads only join the barriers
+// and sums.
+__global__ void __launch_bounds__(1024) post_pressure_kernel(const double* verts, const void* mat, int mat_fp64, int dim,
+                                     int np, const double* pb, const double* u, const double* dudt,
+                                     Modes ms, double t, double* acc) {
+  extern __shared__ double ps[];
+  const int m = np + 1, me = m + 1, F = dim + 1;
+  int N = 1, Mp = 1, Me = 1;
+  for (int d = 0; d < dim; ++d) {
+    N *= np;
+    Mp *= m;
+    Me *= me;
+  }
+  const int64_t c = blockIdx.x;
+  const int i = threadIdx.x;
+  const bool act = i < Mp;
+  const double* interp = pb;
+  const double* qx = pb + m * np;
+  const double* qw = qx + m;
+  const double* D = qw + m;
+  const double* Ie = D + m * m;
+  const double* ex = Ie + me * m;
+  const double* ew = ex + me;
+  double* jxw = ps;
+  double* met = jxw + Mp;        // 6 per point: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2)
+  double* x = met + 6 * Mp;
+  double* z = x + Mp;
+  double* g = z + Mp;            // dim x Mp
+  double* red = g + 3 * Mp;      // 33
+  const double* V = verts + c * (1 << dim) * dim;
+  const double rho_c = mat_fp64 ? static_cast<const double*>(mat)[4 * c]
+                                 : (double)static_cast<const float*>(mat)[4 * c];
+  int ii[3] = {0, 0, 0};
+  {
+    int q = i;
+    for (int e = 0; e < dim; ++e) {
+      ii[e] = q % m;
+      q /= m;
+    }
+  }
+  const int str[3] = {1, m, m * m};
+  // geometry, du/dt and p at this thread's point
+  double xi[3] = {0, 0, 0}, w = 1.0;
+  for (int e = 0; e < dim; ++e) {
+    xi[e] = qx[ii[e]];
+    w *= qw[ii[e]];
+  }
+  double JiT[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  const double jw = act ? fabs(jac_inv_t_dev(dim, V, xi, JiT)) * w : 0.0;
+  double vt[3] = {0, 0, 0}, pq = 0.0;
+  if (act) {
+    jxw[i] = jw;
+    double mt[3][3];
+    for (int e = 0; e < 3; ++e)
+      for (int f = 0; f < 3; ++f) {
+        double s = 0.0;
+        for (int d = 0; d < dim; ++d) s += JiT[d][e] * JiT[d][f];
+        mt[e][f] = jw * s;
+      }
+    met[6 * i + 0] = mt[0][0];
+    met[6 * i + 1] = mt[1][1];
+    met[6 * i + 2] = mt[2][2];
+    met[6 * i + 3] = mt[0][1];
+    met[6 * i + 4] = mt[0][2];
+    met[6 * i + 5] = mt[1][2];
+    for (int q = 0; q < N; ++q) {
+      int qq = q;
+      double wgt = 1.0;
+      for (int e = 0; e < dim; ++e) {
+        wgt *= interp[ii[e] * np + qq % np];
+        qq /= np;
+      }
+      for (int d = 0; d < dim; ++d) vt[d] += wgt * dudt[(c * F + d) * N + q];
+      pq += wgt * u[(c * F + dim) * N + q];
+    }
+    // rhs: reference-coordinate flux jxw JiT^T (-rho du/dt), then D^T
+    for (int e = 0; e < dim; ++e) {
+      double s = 0.0;
+      for (int d = 0; d < dim; ++d) s += JiT[d][e] * (-rho_c * vt[d]);
+      g[e * Mp + i] = jw * s;
+    }
+  }
+  __syncthreads();
+  auto dtrans = [&](int idx) {
+    double s = 0.0;
+    for (int e = 0; e < dim; ++e)
+      for (int a = 0; a < m; ++a) s += D[a * m + ii[e]] * g[e * Mp + idx + (a - ii[e]) * str[e]];
+    return s;
+  };
+  const double rhs_i = (i == 0 || !act) ? 0.0 : dtrans(i);
+  const double vol = block_sum_all(jw, red);
+  const double pint = block_sum_all(jw * pq, red);
+  // SolverCGvect::solve (elementwise_cg.templates.h:64-145)
+  const double ABS_TOL = 1e-20, REL_TOL = 1e-11;
+  double xi_v = 0.0;
+  double ri = rhs_i;
+  const double r0 = sqrt(block_sum_all(ri * ri, red));
+  if (r0 > 0.0) {
+    double pi_v = ri;
+    double ry = block_sum_all(ri * pi_v, red);
+    for (int it = 1; it <= 6 * Mp; ++it) {
+      // v = K p with unknown 0 constrained
+      if (act) z[i] = (i == 0) ? 0.0 : pi_v;
+      __syncthreads();
+      double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+      if (act) {
+        double gr[3] = {0, 0, 0};
+        for (int e = 0; e < dim; ++e)
+          for (int a = 0; a < m; ++a) gr[e] += D[ii[e] * m + a] * z[i + (a - ii[e]) * str[e]];
+        const double* mt = met + 6 * i;
+        g0 = mt[0] * gr[0] + mt[3] * gr[1] + mt[4] * gr[2];
+        g1 = mt[3] * gr[0] + mt[1] * gr[1] + mt[5] * gr[2];
+        g2 = mt[4] * gr[0] + mt[5] * gr[1] + mt[2] * gr[2];
+      }
+      __syncthreads();
+      if (act) {
+        g[i] = g0;
+        if (dim > 1) g[Mp + i] = g1;
+        if (dim > 2) g[2 * Mp + i] = g2;
+      }
+      __syncthreads();
+      const double vi = !act ? 0.0 : (i == 0) ? pi_v : dtrans(i);
+      double pvv = block_sum_all(pi_v * vi, red);
+      if (fabs(pvv) < ABS_TOL) pvv = ABS_TOL;
+      const double alpha = ry / pvv;
+      xi_v += alpha * pi_v;
+      ri -= alpha * vi;
+      const double rr = block_sum_all(ri * ri, red);
+      const double rn = sqrt(rr);
+      if (rn < ABS_TOL || rn / r0 < REL_TOL) break;
+      const double beta = rr / ry;
+      pi_v = ri + beta * pi_v;
+      ry = rr;
+    }
+  }
+  // mean of p
+  const double sint = block_sum_all(jw * xi_v, red);
+  if (act) x[i] = xi_v + (pint - sint) / vol;
+  __syncthreads();
+  // L2 error with QGauss(k+3)
+  double es = 0.0;
+  for (int q = i; q < Me; q += blockDim.x) {
+    int ie[3] = {0, 0, 0}, tq = q;
+    double xe[3] = {0, 0, 0}, we = 1.0;
+    for (int e = 0; e < dim; ++e) {
+      ie[e] = tq % me;
+      tq /= me;
+      xe[e] = ex[ie[e]];
+      we *= ew[ie[e]];
+    }
+    double val = 0.0;
+    for (int a = 0; a < Mp; ++a) {
+      int aa = a;
+      double wgt = 1.0;
+      for (int e = 0; e < dim; ++e) {
+        wgt *= Ie[ie[e] * m + aa % m];
+        aa /= m;
+      }
+      val += wgt * x[a];
+    }
+    double xp[3] = {0, 0, 0}, exv[4];
+    map_point_dev(dim, V, xe, xp);
+    membrane_dev(dim, ms, xp, t, exv);
+    const double d = val - exv[dim];
+    es += d * d * fabs(jac_det_dev(dim, V, xe)) * we;
+  }
+  const double tot = block_sum_all(es, red);
+  if (i == 0) atomicAdd(acc + 3, tot);
+}
+
 int grid_for(int64_t n) {
   const int64_t b = (n + 255) / 256;
   return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 1 << 20);
@@ -338,7 +567,9 @@ struct ew_ctx {
   int32_t* d_rec_cell = nullptr;
   double* d_rec_w = nullptr;
   // ADERADCONFULL: two FP64 vectors for the repeated operator applications
+  // (the first also holds du/dt of the post-processing)
   double* d_ad[2] = {nullptr, nullptr};
+  double* d_post = nullptr;  // basis data of the post-processing (QGauss(k+2), QGauss(k+3))
   std::string last_error;
   int64_t launches = 0;
 };
@@ -382,7 +613,7 @@ void free_ctx(ew_ctx* c) {
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
                   c->d_work_stage, c->d_work_ck, c->d_work_cart, c->d_cellc, c->d_err, c->d_tmp64, c->d_x32[0],
-                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w, c->d_ad[0], c->d_ad[1]};
+                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w, c->d_ad[0], c->d_ad[1], c->d_post};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -1347,6 +1578,61 @@ int ew_sample_receivers(ew_ctx* ctx, const double* state, double* out) {
   ++ctx->launches;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "receiver launch");
+}
+
+int ew_l2_error_post_membrane(ew_ctx* ctx, const double* state, int32_t n_modes,
+                               const double* amps, const int32_t* kvecs, double t, double* out) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!state || !out) return fail(ctx, EW_ERR_INVALID, "ew_l2_error_post_membrane: NULL argument");
+  ew::Modes ms;
+  if ((rc = make_modes(ctx, n_modes, amps, kvecs, &ms))) return rc;
+  const int dim = ctx->dim, np = ctx->np, m = np + 1, me = m + 1;
+  int Mp = 1;
+  for (int d = 0; d < dim; ++d) Mp *= m;
+  if (!ctx->d_post) {
+    // interp (m x np), qx, qw, D (m x m), Ie (me x m), ex, ew
+    const ew::GaussRule g = ew::gauss_rule(np), gp = ew::gauss_rule(m), ge = ew::gauss_rule(me);
+    std::vector<double> pb;
+    for (int a = 0; a < m; ++a)
+      for (int i = 0; i < np; ++i) pb.push_back(ew::lagrange(g.x, i, gp.x[a]));
+    pb.insert(pb.end(), gp.x.begin(), gp.x.end());
+    pb.insert(pb.end(), gp.w.begin(), gp.w.end());
+    for (int a = 0; a < m; ++a)
+      for (int j = 0; j < m; ++j) pb.push_back(ew::lagrange_deriv(gp.x, j, gp.x[a]));
+    for (int a = 0; a < me; ++a)
+      for (int j = 0; j < m; ++j) pb.push_back(ew::lagrange(gp.x, j, ge.x[a]));
+    pb.insert(pb.end(), ge.x.begin(), ge.x.end());
+    pb.insert(pb.end(), ge.w.begin(), ge.w.end());
+    if ((rc = dev_alloc(ctx, &ctx->d_post, pb.size())) ||
+        (rc = upload(ctx, ctx->d_post, pb.data(), pb.size() * 8)))
+      return rc;
+  }
+  if (!ctx->d_ad[0] && (rc = dev_alloc(ctx, &ctx->d_ad[0], (size_t)ctx->n_dofs))) return rc;
+  // du/dt = M^-1 A(u) (its velocity part feeds the right-hand side)
+  const int var = ctx->mixed ? ew::STAGE_MIX_IN64 : ew::STAGE_F64;
+  const int cv = ctx->mixed ? ew::CV_MIX_APPLY64 : ew::CV_F64_APPLY;
+  if ((rc = launch_stage(ctx, var, cv, nullptr, state, nullptr, ctx->d_ad[0], ew::MODE_APPLY, 0.0,
+                         0.0, 1.0f)))
+    return rc;
+  cudaError_t e = cudaMemsetAsync(ctx->d_acc, 0, 4 * sizeof(double), ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
+  const size_t smem = ((size_t)12 * Mp + 33) * sizeof(double);
+  if (smem > 48 * 1024 &&
+      (e = cudaFuncSetAttribute(ew::post_pressure_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem)) != cudaSuccess)
+    return cuda_fail(ctx, e, "post kernel attribute");
+  ew::post_pressure_kernel<<<(unsigned)ctx->n_cells, (Mp + 31) / 32 * 32, smem, ctx->stream>>>(
+      ctx->d_verts, ctx->d_mat, ctx->mixed ? 0 : 1, dim, np, ctx->d_post, state, ctx->d_ad[0], ms, t,
+      ctx->d_acc);
+  ++ctx->launches;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "post kernel launch");
+  double h[4];
+  e = cudaMemcpyAsync(h, ctx->d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "post readback");
+  *out = std::sqrt(h[3]);
+  return EW_OK;
 }
 
 int ew_synchronize(ew_ctx* ctx) {

@@ -11,8 +11,8 @@ SUPPORTED = {"LSRK45R2": LowStorageRK45Reg2, "clRK4": ClassRK4, "ADER": Arbitrar
 
 
 def run(params, precision="fp64", on_output=None):
-    """Run the parameter set; returns rows (time, step, err p, err u, |p|)
-    and the time step used.  ``params`` as returned by parameters.parse_prm."""
+    """Run the parameter set; returns rows (time, step, err p, err u, |p|,
+    err p post) and the time step used.  ``params`` as returned by parameters.parse_prm."""
     import torch
     integ = params["time_integrator"]
     if integ not in SUPPORTED:
@@ -37,7 +37,8 @@ def run(params, precision="fp64", on_output=None):
 
     def output():
         e = op.l2_errors(sol, amps, kv, tc.time)
-        rows.append((tc.time, tc.time_step_number, e[0], e[1], e[2]))
+        post = op.l2_error_post(sol, amps, kv, tc.time)
+        rows.append((tc.time, tc.time_step_number, e[0], e[1], e[2], post))
         if on_output:
             on_output(rows[-1])
 

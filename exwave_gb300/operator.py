@@ -156,6 +156,15 @@ class WaveEquationOperation:
                                                kv.ctypes.data, t, out.ctypes.data))
         return out
 
+    def l2_error_post(self, u, amps, kvecs, t):
+        """L2 error of the post-processed pressure of degree k+1 (compute_post_pressure,
+        wave_equation_operations.cc:784-848; explicit_wave.cc:476-484)."""
+        a, kv = _modes(amps, kvecs)
+        out = np.zeros(1)
+        self._chk(self.L.ew_l2_error_post_membrane(self.ctx, _ptr(u), len(a), a.ctypes.data,
+                                                   kv.ctypes.data, t, out.ctypes.data))
+        return float(out[0])
+
     def l2_difference(self, a, b):
         out = np.zeros(2)
         self._chk(self.L.ew_l2_difference(self.ctx, _ptr(a), _ptr(b), out.ctypes.data))

@@ -194,6 +194,17 @@ int ew_project_gaussian(ew_ctx* ctx, const double* x0, double width, double amp,
 int ew_l2_errors_membrane(ew_ctx* ctx, const double* u, int32_t n_modes, const double* amp,
                           const int32_t* kvec, double t, double out[3]);
 
+/* "error p post": the post-processed pressure p* of degree k+1 per cell
+ * (WaveEquationOperation::compute_post_pressure,
+ * wave_equation_operations.cc:784-848: (grad phi, grad p*) =
+ * (grad phi, -rho du/dt) with QGauss(k+2), du/dt = M^-1 A(u), one value
+ * constrained, CG to 1e-11, then shifted to the mean of p_h) and its L2
+ * error against the membrane pressure with QGauss(k+3)
+ * (explicit_wave.cc:476-484).  FP64 throughout except du/dt and the
+ * density, which a mixed context holds in FP32.  Synchronises. */
+int ew_l2_error_post_membrane(ew_ctx* ctx, const double* state, int32_t n_modes,
+                              const double* amps, const int32_t* kvecs, double t, double* out);
+
 /* L2 norm of the difference of two states with QGauss(k+2) (pressure,
  * velocity); used for FP64-vs-mixed comparisons.  Synchronises. */
 int ew_l2_difference(ew_ctx* ctx, const double* a, const double* b, double out[2]);
