@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cells", type=int, default=64)
     ap.add_argument("--degree", type=int, default=5)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cells-per-block", type=int, default=0,
+                    help="cells per thread block of the operator kernel (0: tuned value)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -549,7 +551,8 @@ def main():
         peaks = json.load(f)
     peak, peak_kind = float(peaks["hbm_gbs"]), "measured"
     m, dt = build_problem(args.cells, args.degree)
-    op = ew.WaveEquationOperation(m, args.degree, precision=args.precision, device=local)
+    op = ew.WaveEquationOperation(m, args.degree, precision=args.precision, device=local,
+                                  cells_per_block=args.cells_per_block)
     n = op.n_dofs
     with ClockSampler(local) as clk:
         ms, launches, errs, _ = time_steps(op, dt, args.steps, args.warmup, torch, barrier)

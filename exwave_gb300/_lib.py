@@ -28,7 +28,7 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches",
            "ew_tune_set", "ew_tune_get", "ew_lsrk45_step_static", "ew_lsrk45_steps",
            "ew_set_receivers", "ew_sample_receivers", "ew_aderadconfull_step",
-           "ew_l2_error_post_membrane"]
+           "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update"]
 
 
 class EwError(RuntimeError):
@@ -94,6 +94,8 @@ def load():
         "ew_project_gaussian": (ctypes.c_int, [vp, dp, d, d, dp]),
         "ew_l2_errors_membrane": (ctypes.c_int, [vp, dp, i32, dp, i32p, d, dp]),
         "ew_l2_error_post_membrane": (ctypes.c_int, [vp, dp, i32, dp, i32p, d, dp]),
+        "ew_lsrk_step": (ctypes.c_int, [vp, i32, d, dp, dp]),
+        "ew_vec_update": (ctypes.c_int, [vp, d, dp, d, dp, d, dp]),
         "ew_l2_difference": (ctypes.c_int, [vp, dp, dp, dp]),
         "ew_hypercube_n_cells": (i64, [ctypes.POINTER(HypercubeDesc)]),
         "ew_hypercube_mesh": (ctypes.c_int, [ctypes.POINTER(HypercubeDesc), dp, i32p]),

@@ -89,6 +89,17 @@ __global__ void axpy_kernel(int64_t n, double c, const double* x, double* y) {
     y[i] += c * x[i];
 }
 
+// y = alpha y + (beta x + gamma z); a NULL x or z drops its term, alpha == 0
+// does not read y
+__global__ void vec_update_kernel(int64_t n, double alpha, double* y, double beta, const double* x,
+                                  double gamma, const double* z) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double xz = (x ? beta * x[i] : 0.0) + (z ? gamma * z[i] : 0.0);
+    y[i] = alpha == 0.0 ? xz : alpha * y[i] + xz;
+  }
+}
+
 __global__ void rk_update_kernel(int64_t n, double f1, double f2, int is_last, const double* v1,
                                  double* v2, double* v3) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -1191,6 +1202,137 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
     if (rc) return rc;
   }
   return EW_OK;
+}
+
+int ew_vec_update(ew_ctx* ctx, double alpha, double* y, double beta, const double* x, double gamma,
+                  const double* z) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!y) return fail(ctx, EW_ERR_INVALID, "ew_vec_update: NULL output");
+  ew::vec_update_kernel<<<ew::grid_for(ctx->n_dofs), 256, 0, ctx->stream>>>(ctx->n_dofs, alpha, y,
+                                                                           beta, x, gamma, z);
+  ++ctx->launches;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "vec_update launch");
+}
+
+namespace {
+// Coefficients of the low-storage 2-register schemes: a_{s+1,s} (n-1 of
+// them) and b_s (n).  LowStorageRK33Reg2 (time_integrators.cc:206-211),
+// LowStorageRK59Reg2 (time_integrators.cc:294-311).
+struct Lsrk2r {
+  int n;
+  double a[8];
+  double b[9];
+};
+const Lsrk2r kLsrk33 = {3,
+                        {0.755726351946097, 0.386954477304099},
+                        {0.245170287303492, 0.184896052186740, 0.569933660509768}};
+const Lsrk2r kLsrk59 = {
+    9,
+    {1107026461565. / 5417078080134., 38141181049399. / 41724347789894.,
+     493273079041. / 11940823631197., 1851571280403. / 6147804934346.,
+     11782306865191. / 62590030070788., 9452544825720. / 13648368537481.,
+     4435885630781. / 26285702406235., 2357909744247. / 11371140753790.},
+    {2274579626619. / 23610510767302., 693987741272. / 12394497460941.,
+     -347131529483. / 15096185902911., 1144057200723. / 32081666971178.,
+     1562491064753. / 11797114684756., 13113619727965. / 44346030145118.,
+     393957816125. / 7825732611452., 720647959663. / 6565743875477.,
+     3559252274877. / 14424734981077.}};
+
+// Register plan of the fused FP64 stages over three vectors (0 = vec_n,
+// 1 = vec_np, 2 = scratch).  Stage 0 reads the state (0) as input and
+// accumulator and writes both outputs to 1 and 2; later stages read X (from
+// neighbouring cells: never written in the same launch) and A (cell-local:
+// one output may overwrite it in place) and write the other output to the
+// third vector.  One choice per stage; the plan is the first whose last
+// stage leaves the result in vec_np.
+struct StagePlan {
+  int X, A, Xo, Ao;
+};
+bool plan_2r(int n, StagePlan* plan) {
+  for (int mask = 0; mask < (1 << n); ++mask) {
+    int X = 0, A = 0;
+    for (int s = 0; s < n; ++s) {
+      const bool bit = (mask >> s) & 1;
+      StagePlan& p = plan[s];
+      p.X = X;
+      p.A = A;
+      if (s == 0) {
+        p.Xo = n == 1 ? -1 : (bit ? 1 : 2);
+        p.Ao = n == 1 ? 1 : 3 - (bit ? 1 : 2);
+      } else {
+        const int F = 3 - X - A;
+        if (s + 1 < n) {
+          p.Xo = bit ? A : F;
+          p.Ao = bit ? F : A;
+        } else {
+          p.Xo = -1;
+          p.Ao = bit ? F : A;
+        }
+      }
+      X = p.Xo;
+      A = p.Ao;
+    }
+    if (plan[n - 1].Ao == 1) return true;
+  }
+  return false;
+}
+
+int lsrk2r_step(ew_ctx* ctx, const Lsrk2r& sc, double dt, double* vec_n, double* vec_np) {
+  using namespace ew;
+  const int n = sc.n;
+  double f1[9], f2[9];
+  for (int s = 0; s + 1 < n; ++s) {
+    f1[s] = sc.a[s] * dt;
+    f2[s] = (sc.b[s] - sc.a[s]) * dt;
+  }
+  f1[n - 1] = sc.b[n - 1] * dt;
+  f2[n - 1] = 0.0;
+  int rc;
+  if (!ctx->mixed) {
+    StagePlan plan[9];
+    if (!plan_2r(n, plan)) return fail(ctx, EW_ERR_UNSUPPORTED, "no register plan for the scheme");
+    double* R[3] = {vec_n, vec_np, ctx->d_tmp64};
+    for (int s = 0; s < n; ++s) {
+      const StagePlan& p = plan[s];
+      const bool last = s + 1 == n;
+      rc = launch_stage(ctx, STAGE_F64, last ? CV_F64_LAST : CV_F64_MID, R[p.A], R[p.X],
+                        last ? nullptr : R[p.Xo], R[p.Ao], last ? MODE_RK_LAST : MODE_RK_MID, f1[s],
+                        f2[s], 1.0f);
+      if (rc) return rc;
+    }
+    return EW_OK;
+  }
+  // mixed: the accumulator in vec_np (in place), FP32 stage inputs ping-pong
+  float* xb[2] = {ctx->d_x32[0], ctx->d_x32[1]};
+  rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, xb[0], vec_np, MODE_RK_MID, f1[0],
+                    f2[0], 1.0f);
+  if (rc) return rc;
+  int cur = 0;
+  for (int s = 1; s < n; ++s) {
+    const bool last = s + 1 == n;
+    rc = launch_stage(ctx, STAGE_MIX_IN32, last ? CV_MIX_LAST : CV_MIX_MID, vec_np, xb[cur],
+                      last ? nullptr : xb[cur ^ 1], vec_np, last ? MODE_RK_LAST : MODE_RK_MID, f1[s],
+                      f2[s], 1.0f);
+    if (rc) return rc;
+    cur ^= 1;
+  }
+  return EW_OK;
+}
+}  // namespace
+
+int ew_lsrk_step(ew_ctx* ctx, int32_t scheme, double dt, double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_lsrk_step: vec_n and vec_np must be distinct");
+  switch (scheme) {
+    case EW_LSRK33R2: return lsrk2r_step(ctx, kLsrk33, dt, vec_n, vec_np);
+    case EW_LSRK45R2: return ew_lsrk45_step(ctx, dt, vec_n, vec_np);
+    case EW_LSRK59R2: return lsrk2r_step(ctx, kLsrk59, dt, vec_n, vec_np);
+    default: return fail(ctx, EW_ERR_INVALID, "ew_lsrk_step: unknown scheme");
+  }
 }
 
 int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, double* vec_np) {

@@ -3,10 +3,15 @@
 output of L2 errors at every tick."""
 from . import mesh as mesh_mod
 from .operator import WaveEquationOperation, reference_mode
-from .time_integrators import AderAdconFull, ArbitraryHighOrderDG, ClassRK4, LowStorageRK45Reg2
+from .time_integrators import (SSPRK, AderAdconFull, ArbitraryHighOrderDG, ClassRK4, ExplicitEuler,
+                               LowStorageRK33Reg2, LowStorageRK45Reg2, LowStorageRK45Reg3,
+                               LowStorageRK59Reg2)
 from .utilities import TimeControl
 
-SUPPORTED = {"LSRK45R2": LowStorageRK45Reg2, "clRK4": ClassRK4, "ADER": ArbitraryHighOrderDG,
+# the integrators of parameters.cc:58 except ADERLTS (local time stepping)
+SUPPORTED = {"ExplEuler": ExplicitEuler, "clRK4": ClassRK4, "LSRK45R2": LowStorageRK45Reg2,
+             "LSRK33R2": LowStorageRK33Reg2, "LSRK45R3": LowStorageRK45Reg3,
+             "LSRK59R2": LowStorageRK59Reg2, "SSPRK": SSPRK, "ADER": ArbitraryHighOrderDG,
              "ADERADCONFULL": AderAdconFull}
 
 

@@ -104,6 +104,19 @@ class WaveEquationOperation:
     def lsrk45_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_lsrk45_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 
+    LSRK_SCHEMES = {"LSRK33R2": 0, "LSRK45R2": 1, "LSRK59R2": 2}
+
+    def lsrk_step(self, scheme, dt, vec_n, vec_np):
+        """One step of a low-storage 2-register scheme (LSRK33R2, LSRK45R2, LSRK59R2)."""
+        self._chk(self.L.ew_lsrk_step(self.ctx, self.LSRK_SCHEMES[scheme], dt, _ptr(vec_n),
+                                      _ptr(vec_np)))
+
+    def vec_update(self, alpha, y, beta=0.0, x=None, gamma=0.0, z=None):
+        """y = alpha*y + (beta*x + gamma*z) on the device (x or z None: term dropped)."""
+        self._chk(self.L.ew_vec_update(self.ctx, alpha, _ptr(y), beta,
+                                       None if x is None else _ptr(x), gamma,
+                                       None if z is None else _ptr(z)))
+
     def lsrk45_steps(self, dt, n_steps, vec_n, vec_np):
         """n_steps LSRK45 steps in one call (vec_n in, clobbered; vec_np out)."""
         self._chk(self.L.ew_lsrk45_steps(self.ctx, dt, int(n_steps), _ptr(vec_n), _ptr(vec_np)))

@@ -116,6 +116,24 @@ int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const doubl
  * the reference. */
 int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
 
+/* Low-storage 2-register schemes of the reference, selected by
+ * ew_lsrk_scheme: replaces LowStorageRK33Reg2 (time_integrators.cc:200-233),
+ * LowStorageRK45Reg2 (:235-283, the same as ew_lsrk45_step) and
+ * LowStorageRK59Reg2 (:286-364)::perform_time_step.  One fused
+ * operator+update launch per stage; vec_n is used as a register, the new
+ * state is left in vec_np. */
+typedef enum ew_lsrk_scheme { EW_LSRK33R2 = 0, EW_LSRK45R2 = 1, EW_LSRK59R2 = 2 } ew_lsrk_scheme;
+int ew_lsrk_step(ew_ctx* ctx, int32_t scheme, double dt, double* vec_n, double* vec_np);
+
+/* y = alpha*y + (beta*x + gamma*z) over the context's n_dofs: the vector
+ * operations of the reference's composed integrators (deal.II Vector::add
+ * with alpha = 1, Vector::sadd with gamma = 0, assignment with alpha = 0 and
+ * beta = 1), used by ExplicitEuler, ClassRK4, LowStorageRK45Reg3 and SSPRK
+ * (time_integrators.cc:24-31, 66-102, 366-427, 440-478).  A NULL x or z
+ * drops its term; alpha == 0 does not read y.  All device vectors. */
+int ew_vec_update(ew_ctx* ctx, double alpha, double* y, double beta, const double* x, double gamma,
+                  const double* z);
+
 /* n_steps LSRK45 steps in one call: the reference's time loop
  * (explicit_wave.cc:779-799) calling perform_time_step and swapping the two
  * vectors n_steps times.  On entry vec_n holds u^n; on return vec_np holds

@@ -1139,6 +1139,147 @@ void ewo_clrk4_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
   for (int64_t i = 0; i < nd; ++i) vec_np[i] += dt / 6. * t1[i];
 }
 
+// ExplicitEuler::perform_time_step (time_integrators.cc:24-31):
+// vec_np = M^-1 A(vec_n), then vec_np = dt vec_np + vec_n (Vector::sadd).
+void ewo_expleuler_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  const int64_t nd = (int64_t)O->n_dofs();
+  O->apply(vec_n, vec_np);
+  for (int64_t i = 0; i < nd; ++i) vec_np[i] = dt * vec_np[i] + vec_n[i];
+}
+
+// Low-storage 2-register schemes in the form of LowStorageRK33Reg2 /
+// LowStorageRK45Reg2 / LowStorageRK59Reg2 (time_integrators.cc:200-364):
+// stage s applies the operator to the current stage input and calls the
+// RKVectorUpdater with (a_{s+1,s} dt, (b_s - a_{s+1,s}) dt); the roles of
+// vec_n and vec_np alternate, the last stage adds b_n dt.  a[n-1], b[n].
+static void lsrk2r_step(Oracle* O, int n, const double* a, const double* b, double dt,
+                        double* vec_n, double* vec_np) {
+  const int64_t nd = (int64_t)O->n_dofs();
+  std::vector<double> tmp(nd);
+  for (int s = 0; s < n; ++s) {
+    // stage input: vec_n in the first stage, then the vector the previous
+    // update wrote as its second argument (vec_n after even, vec_np after
+    // odd stages)
+    const double* in = (s == 0 || (s & 1)) ? vec_n : vec_np;
+    O->apply(in, tmp.data());
+    if (s + 1 == n)
+      ewo_rk_update(nd, b[s] * dt, 0.0, 1, tmp.data(), vec_np, vec_n);
+    else if (s & 1)
+      ewo_rk_update(nd, a[s] * dt, (b[s] - a[s]) * dt, 0, tmp.data(), vec_np, vec_n);
+    else
+      ewo_rk_update(nd, a[s] * dt, (b[s] - a[s]) * dt, 0, tmp.data(), vec_n, vec_np);
+  }
+}
+
+// LowStorageRK33Reg2 coefficients (time_integrators.cc:206-211)
+void ewo_lsrk33_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
+  const double a[2] = {0.755726351946097, 0.386954477304099};
+  const double b[3] = {0.245170287303492, 0.184896052186740, 0.569933660509768};
+  lsrk2r_step(reinterpret_cast<Oracle*>(p), 3, a, b, dt, vec_n, vec_np);
+}
+
+// LowStorageRK59Reg2 coefficients (time_integrators.cc:294-311)
+void ewo_lsrk59_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
+  const double a[8] = {1107026461565. / 5417078080134.,   38141181049399. / 41724347789894.,
+                       493273079041. / 11940823631197.,   1851571280403. / 6147804934346.,
+                       11782306865191. / 62590030070788., 9452544825720. / 13648368537481.,
+                       4435885630781. / 26285702406235.,  2357909744247. / 11371140753790.};
+  const double b[9] = {2274579626619. / 23610510767302.,  693987741272. / 12394497460941.,
+                       -347131529483. / 15096185902911.,  1144057200723. / 32081666971178.,
+                       1562491064753. / 11797114684756.,  13113619727965. / 44346030145118.,
+                       393957816125. / 7825732611452.,    720647959663. / 6565743875477.,
+                       3559252274877. / 14424734981077.};
+  lsrk2r_step(reinterpret_cast<Oracle*>(p), 9, a, b, dt, vec_n, vec_np);
+}
+
+// y = alpha y + (beta x + gamma z): Vector::add(a, V, b, W) (alpha = 1),
+// Vector::sadd(s, a, V) (gamma = 0) and assignment (alpha = 0, beta = 1)
+static void vec_update(int64_t n, double alpha, double* y, double beta, const double* x,
+                       double gamma, const double* z) {
+  for (int64_t i = 0; i < n; ++i) {
+    const double xz = (x ? beta * x[i] : 0.0) + (z ? gamma * z[i] : 0.0);
+    y[i] = alpha == 0.0 ? xz : alpha * y[i] + xz;
+  }
+}
+
+// LowStorageRK45Reg3::perform_time_step (time_integrators.cc:366-427),
+// the same sequence of operator applications and vector operations.
+void ewo_lsrk45r3_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  const int64_t nd = (int64_t)O->n_dofs();
+  const double a21 = 2365592473904. / 8146167614645., a32 = 4278267785271. / 6823155464066.,
+               a43 = 2789585899612. / 8986505720531., a54 = 15310836689591. / 24358012670437.;
+  const double a31 = -722262345248. / 10870640012513., a42 = 1365858020701. / 8494387045469.,
+               a53 = 3819021186. / 2763618202291.;
+  const double b1 = 846876320697. / 6523801458457., b2 = 3032295699695. / 12397907741132.,
+               b3 = 612618101729. / 6534652265123., b4 = 1155491934595. / 2954287928812.,
+               b5 = 707644755468. / 5028292464395.;
+  std::vector<double> t1(nd), t2(nd);
+  O->apply(vec_n, vec_np);
+  vec_update(nd, 1.0, vec_n, a21 * dt, vec_np, 0.0, nullptr);
+  vec_update(nd, 0.0, t1.data(), 1.0, vec_n, 0.0, nullptr);
+  vec_update(nd, 1.0, t1.data(), (b1 - a21) * dt, vec_np, 0.0, nullptr);
+  O->apply(vec_n, t2.data());
+  vec_update(nd, 1.0, t1.data(), a32 * dt, t2.data(), (a31 - b1) * dt, vec_np);
+  vec_update(nd, (b1 - a31) * dt, vec_np, 1.0, t1.data(), 0.0, nullptr);
+  vec_update(nd, 1.0, vec_np, (b2 - a32) * dt, t2.data(), 0.0, nullptr);
+  O->apply(t1.data(), vec_n);
+  vec_update(nd, 1.0, vec_np, a43 * dt, vec_n, (a42 - b2) * dt, t2.data());
+  vec_update(nd, (b2 - a42) * dt, t2.data(), 1.0, vec_np, 0.0, nullptr);
+  vec_update(nd, 1.0, t2.data(), (b3 - a43) * dt, vec_n, 0.0, nullptr);
+  O->apply(vec_np, t1.data());
+  vec_update(nd, 1.0, t2.data(), a54 * dt, t1.data(), (a53 - b3) * dt, vec_n);
+  vec_update(nd, 0.0, vec_np, 1.0, t2.data(), 0.0, nullptr);
+  vec_update(nd, 1.0, vec_np, (b3 - a53) * dt, vec_n, (b4 - a54) * dt, t1.data());
+  O->apply(t2.data(), t1.data());
+  vec_update(nd, 1.0, vec_np, b5 * dt, t1.data(), 0.0, nullptr);
+}
+
+// SSPRK(order 4, 8 stages), SSPRK::perform_time_step (time_integrators.cc:440-478)
+// with the coefficients of initialize_coeffs (time_integrators.cc:726-795):
+// u_s = sum_{l<s} A[s-1][l] u_l + dt B[s-1][l] M^-1 A(u_l), u_0 = vec_n,
+// vec_np = u_8.  Rows are listed as (l, A, B) for the nonzero entries.
+struct SspTerm {
+  int l;
+  double a, b;
+};
+static const SspTerm kSsp48[8][8] = {
+    {{0, 1., 0.282318339066479}},
+    {{0, 0.538569155333175, 0.}, {1, 0.461430844666825, 0.130270389660380}},
+    {{0, 0.004485387460763, 0.003963092203460}, {2, 0.995514612539237, 0.281052031928487}},
+    {{0, 0.164495299288580, 0.000038019518678}, {1, 0.016875060685979, 0.004764139104512},
+     {3, 0.818629640025440, 0.231114160282572}},
+    {{0, 0.426933682982668, 0.000019921336144}, {1, 0.157047028197878, 0.044337256156151},
+     {2, 0.023164224070770, 0.006539685265423}, {4, 0.392855064748685, 0.110910189373703}},
+    {{0, 0.082083400476958, 0.000000034006679}, {1, 0.000000039091042, 0.000000011036118},
+     {2, 0.033974171137350, 0.009591531566657}, {3, 0.005505195713107, 0.001554217709960},
+     {5, 0.878437193581543, 0.247998929466160}},
+    {{0, 0.006736365648625, 0.013159891155054}, {1, 0.010581829625529, 0.002987444564164},
+     {2, 0.009353386191951, 0.002640632454359}, {3, 0.101886062556838, 0.028764303955070},
+     {4, 0.000023428364930, 0.000006614257074}, {6, 0.871418927612128, 0.246017544274548}},
+    {{0, 0.071115287415749, 0.000000010647874}, {1, 0.018677648343953, 0.005273042658132},
+     {2, 0.007902408660034, 0.002230994887525}, {3, 0.319384027162348, 0.090167968072837},
+     {4, 0.007121989995845, 0.002010668386475}, {5, 0.001631615692736, 0.000460635032368},
+     {7, 0.574167022729334, 0.162097880203691}}};
+static const int kSsp48Terms[8] = {1, 2, 2, 3, 4, 5, 6, 7};
+
+void ewo_ssprk_step(ewo_problem* p, double dt, double* vec_n, double* vec_np) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  const int64_t nd = (int64_t)O->n_dofs();
+  std::vector<std::vector<double>> u(9, std::vector<double>(nd)), k(8, std::vector<double>(nd));
+  u[0].assign(vec_n, vec_n + nd);
+  for (int s = 1; s <= 8; ++s) {
+    O->apply(u[s - 1].data(), k[s - 1].data());
+    std::fill(u[s].begin(), u[s].end(), 0.0);
+    for (int t = 0; t < kSsp48Terms[s - 1]; ++t) {
+      const SspTerm& c = kSsp48[s - 1][t];
+      vec_update(nd, 1.0, u[s].data(), c.a, u[c.l].data(), c.b * dt, k[c.l].data());
+    }
+  }
+  std::copy(u[8].begin(), u[8].end(), vec_np);
+}
+
 // Time-integrated state of the first ADER step (local_apply_firstader_domain,
 // wave_equation_operations.cc:939-957), written to T.
 void ewo_ader_taylor(ewo_problem* p, double dt, const double* src, double* T) {
@@ -1220,7 +1361,8 @@ void ewo_errors_modes(ewo_problem* p, const double* u, int n_modes, const double
 
 // Replays the reference's time loop (explicit_wave.cc:549-813 with
 // TimeControl, utilities.cc:31-95) for integrator 0 = LSRK45R2, 1 = clRK4,
-// 2 = ADER, 3 = ADERADCONFULL.  cfl is the Courant number as written in the
+// 2 = ADER, 3 = ADERADCONFULL, 4 = ExplEuler, 5 = LSRK33R2, 6 = LSRK45R3,
+// 7 = LSRK59R2, 8 = SSPRK.  cfl is the Courant number as written in the
 // parameter file (divided by k^1.5 here, parameters.cc:195).  Each output
 // tick appends {time, step, err p, err u, |p|} to rows (capacity max_rows);
 // returns the number of rows, or -1 on error.  dt_out receives the
@@ -1250,6 +1392,12 @@ int ewo_run_reference(ewo_problem* p, int integrator, double cfl, double final_t
     ++nrows;
   };
   emit();
+  // TimeControl::setup (utilities.cc:38-46): 0 means the number of steps of
+  // the rounded step size
+  if (max_time_steps == 0) {
+    const double rounded = final_time / std::max(std::round(final_time / dt), 1.0);
+    max_time_steps = (int)std::round(final_time / rounded);
+  }
   while (!(time >= final_time || step > (unsigned)max_time_steps)) {
     ++step;
     time += dt;
@@ -1259,6 +1407,11 @@ int ewo_run_reference(ewo_problem* p, int integrator, double cfl, double final_t
       case 1: ewo_clrk4_step(p, dt, tmp.data(), sol.data()); break;
       case 2: ewo_ader_step(p, dt, tmp.data(), sol.data()); break;
       case 3: ewo_aderadconfull_step(p, dt, tmp.data(), sol.data()); break;
+      case 4: ewo_expleuler_step(p, dt, tmp.data(), sol.data()); break;
+      case 5: ewo_lsrk33_step(p, dt, tmp.data(), sol.data()); break;
+      case 6: ewo_lsrk45r3_step(p, dt, tmp.data(), sol.data()); break;
+      case 7: ewo_lsrk59_step(p, dt, tmp.data(), sol.data()); break;
+      case 8: ewo_ssprk_step(p, dt, tmp.data(), sol.data()); break;
       default: g_last_error = "unknown integrator"; return -1;
     }
     if ((int)(time / tick) != (int)((time - dt) / tick)) emit();

@@ -14,7 +14,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libew_oracle.so")
 
-INTEGRATORS = {"LSRK45R2": 0, "clRK4": 1, "ADER": 2, "ADERADCONFULL": 3}
+INTEGRATORS = {"LSRK45R2": 0, "clRK4": 1, "ADER": 2, "ADERADCONFULL": 3, "ExplEuler": 4,
+               "LSRK33R2": 5, "LSRK45R3": 6, "LSRK59R2": 7, "SSPRK": 8}
+# one step of each integrator: the oracle's entry point
+STEP_FUNCS = {"LSRK45R2": "ewo_lsrk45_step", "clRK4": "ewo_clrk4_step", "ADER": "ewo_ader_step",
+              "ADERADCONFULL": "ewo_aderadconfull_step", "ExplEuler": "ewo_expleuler_step",
+              "LSRK33R2": "ewo_lsrk33_step", "LSRK45R3": "ewo_lsrk45r3_step",
+              "LSRK59R2": "ewo_lsrk59_step", "SSPRK": "ewo_ssprk_step"}
 
 _lib = None
 
@@ -61,8 +67,7 @@ def lib():
         L.ewo_apply.argtypes = [P, dp, dp, ctypes.c_double]
         L.ewo_rk_update.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                     dp, dp, dp]
-        for name in ("ewo_lsrk45_step", "ewo_clrk4_step", "ewo_ader_step",
-                     "ewo_aderadconfull_step", "ewo_ader_taylor", "ewo_apply_ader"):
+        for name in tuple(STEP_FUNCS.values()) + ("ewo_ader_taylor", "ewo_apply_ader"):
             getattr(L, name).argtypes = [P, ctypes.c_double, dp, dp]
         L.ewo_errors_reference.argtypes = [P, dp, ctypes.c_int, ctypes.c_double, dp]
         L.ewo_errors_modes.argtypes = [P, dp, ctypes.c_int, dp, ip, ctypes.c_double, dp]
@@ -168,6 +173,10 @@ class Problem:
 
     def clrk4_step(self, dt, vec_n, vec_np):
         lib().ewo_clrk4_step(self.h, dt, _dp(vec_n), _dp(vec_np))
+
+    def step(self, integrator, dt, vec_n, vec_np):
+        """One perform_time_step of the named integrator (vec_n may be clobbered)."""
+        getattr(lib(), STEP_FUNCS[integrator])(self.h, dt, _dp(vec_n), _dp(vec_np))
 
     def ader_step(self, dt, vec_n, vec_np):
         lib().ewo_ader_step(self.h, dt, _dp(vec_n), _dp(vec_np))
