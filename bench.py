@@ -71,10 +71,8 @@ def parse():
 
 
 def dist_info():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from exwave_gb300.replicas import dist_info as di
+    return di()
 
 
 class ClockSampler:
@@ -521,6 +519,8 @@ def main():
         return
     if args.workload != "membrane3d":
         import torch
+        if dist_info()[1] != 0:
+            return  # the other workloads are single-GPU cases: rank 0 runs them
         from exwave_gb300 import build
         build.build()
         fn = {"ader3d": ader3d, "batch": batch_workload, "serve": serve_workload,
@@ -532,17 +532,10 @@ def main():
         print(json.dumps(res), flush=True)
         return
     import torch
-    ws, rank, local = dist_info()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-
-        def barrier():
-            dist.barrier()
-    else:
-        def barrier():
-            pass
+    from exwave_gb300.replicas import Replicas
+    rep = Replicas("nccl")
+    ws, rank, local = rep.world_size, rep.rank, rep.local_rank
+    barrier = rep.barrier
     import exwave_gb300 as ew
     from exwave_gb300 import build
     build.build()
@@ -556,11 +549,7 @@ def main():
     n = op.n_dofs
     with ClockSampler(local) as clk:
         ms, launches, errs, _ = time_steps(op, dt, args.steps, args.warmup, torch, barrier)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = rep.max(ms)  # the slowest replica times the whole job
     ms_step = ms / args.steps
     value = n * STAGES * args.steps * ws / (ms / 1e3)
     # per launch of stage_cart_kernel: average algorithmic bytes of the five
@@ -590,6 +579,7 @@ def main():
     if not args.no_fp64 and args.precision == "mixed":
         op64 = ew.WaveEquationOperation(m, args.degree, precision="fp64", device=local)
         ms64, _, errs64, _ = time_steps(op64, dt, max(2, args.steps // 4), 1, torch, barrier)
+        ms64 = rep.max(ms64)
         st64 = max(2, args.steps // 4)
         v64 = n * STAGES * st64 * ws / (ms64 / 1e3)
         result["fp64"] = {"value": v64, "ms_per_step": ms64 / st64,
@@ -599,7 +589,9 @@ def main():
         op64.close()
         del op64
     if not args.no_e2e:
+        barrier()
         ms_e, h2d, d2h = e2e_steps(op, dt, args.steps, args.warmup, torch)
+        ms_e = rep.max(ms_e)
         result["e2e"] = {"value": n * STAGES * args.steps * ws / (ms_e / 1e3),
                          "unit": "DoF-updates/s", "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "ms_per_step": ms_e / args.steps}
@@ -610,9 +602,7 @@ def main():
             result["cpu_baseline"] = {"value": None, "error": str(exc)}
     if rank == 0:
         print(json.dumps(result), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
