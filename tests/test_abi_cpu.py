@@ -84,6 +84,30 @@ def test_create_rejects_bad_meshes(lib):
     assert rc == -1
 
 
+def test_create_rejects_degenerate_input(lib):
+    import exwave_gb300 as ew
+    L = lib.load()
+    h = ctypes.c_void_p()
+    # no mesh, no cells, missing arrays
+    assert L.ew_create(None, None, ctypes.byref(h)) == -1
+    m = ew.hypercube(2, 2)
+    md, keep = _mesh_desc(lib, m, 2)
+    md.n_cells = 0
+    assert L.ew_create(ctypes.byref(md), None, ctypes.byref(h)) == -1
+    md, keep = _mesh_desc(lib, m, 2)
+    md.speed = None
+    assert L.ew_create(ctypes.byref(md), None, ctypes.byref(h)) == -1
+    # non-finite material, a collapsed cell
+    bad = ew.hypercube(2, 2)
+    bad.density[1] = float("nan")
+    rc, msg = _create(lib, bad, 2)
+    assert rc == -1 and "positive" in msg
+    bad = ew.hypercube(2, 2)
+    bad.vertices[2] = bad.vertices[2, 0]
+    rc, msg = _create(lib, bad, 2)
+    assert rc == -1
+
+
 @pytest.mark.parametrize("dim,n,ref,f", [(2, 20, 0, 0.0), (2, 5, 2, 0.1), (3, 5, 0, 0.1),
                                          (3, 3, 0, 0.05), (2, 5, 3, 0.1), (3, 2, 2, 0.2)])
 def test_hypercube_matches_oracle(lib, oracle_mod, dim, n, ref, f):

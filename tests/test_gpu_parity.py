@@ -212,3 +212,46 @@ def test_projection_and_errors_match_oracle(env):
     e_gpu = op.l2_errors(u * 1.01, amps, kv, 0.3)
     e_ref = o.errors_modes(ref * 1.01, amps, kv, 0.3)
     np.testing.assert_allclose(e_gpu, e_ref, rtol=1e-12)
+
+
+EDGE = [
+    # dim, k, intervals, transform, boundary ids, cells per block
+    (2, 3, 1, 0.0, [1, 2, 3, 1], 1),      # one cell: every face a boundary
+    (3, 2, 1, 0.1, [3, 1, 2, 2, 1, 3], 1),  # one curved cell
+    (3, 5, 3, 0.0, 2, 4),                  # 27 cells, items of 4: the last holds 3
+    (2, 4, 5, 0.0, [1, 1, 3, 3], 3),      # 25 cells, items of 3: the last holds 1
+    (3, 3, 3, 0.1, 2, 5),                  # curved, 27 cells, items of 5
+]
+
+
+@pytest.mark.parametrize("case", EDGE, ids=lambda c: "d%dk%d_n%d_f%g_cb%d" % (c[0], c[1], c[2], c[3], c[5]))
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ragged_work_lists_and_single_cells(env, case, precision):
+    """Meshes of one cell (all faces on the boundary) and work lists whose
+    last item is only partly filled: apply and three LSRK45 steps against
+    the oracle."""
+    ew, oracle, torch = env
+    dim, k, n, f, bids, cb = case
+    m = ew.hypercube(dim, n, 0, f, boundary_ids=bids)
+    op = ew.WaveEquationOperation(m, k, precision=precision, cells_per_block=cb)
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    rng = np.random.default_rng(77 + k)
+    u = rng.standard_normal(o.n_dofs)
+    ref_out = o.apply(u)
+    src = torch.from_numpy(u).cuda()
+    dst = torch.zeros_like(src)
+    op.apply(src, dst)
+    op.synchronize()
+    err = np.abs(dst.cpu().numpy() - ref_out).max() / np.abs(ref_out).max()
+    assert err < tol, ("apply", err)
+    dt = o.time_step(0.2 / k ** 1.5)
+    a, b = u.copy(), np.zeros_like(u)
+    for _ in range(3):
+        o.lsrk45_step(dt, a, b)
+        a, b = b, a
+    vn, vnp = src.clone(), torch.zeros_like(src)
+    op.lsrk45_steps(dt, 3, vn, vnp)
+    op.synchronize()
+    err = np.abs(vnp.cpu().numpy() - a).max() / np.abs(a).max()
+    assert err < tol, ("lsrk45", err)
