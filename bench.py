@@ -38,7 +38,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 STAGES = 5
-BYTES_PER_DOF_STEP = {"mixed": 112.0, "fp64": 144.0}
+BYTES_PER_DOF_STEP = {"mixed": 112.0, "mixed_ff": 112.0, "fp64": 144.0}
 
 
 def parse():
@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cells", type=int, default=64)
     ap.add_argument("--degree", type=int, default=5)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_ff", "fp64"],
+                    help="mixed: FP32 operator; mixed_ff: compensated (float-float) operator")
     ap.add_argument("--cells-per-block", type=int, default=0,
                     help="cells per thread block of the operator kernel (0: tuned value)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
@@ -370,15 +371,15 @@ def ader3d(args, torch):
 def membrane2d(args, torch):
     """2-D vibrating membrane, 16^2 affine quads, FE_DGQ(4), modes (1,1) +
     0.5 (2,3), p = 0 on the boundary, LSRK45 with dt = 2^-9, 512 steps to
-    T = 1, FP64 and mixed: time of the whole run (one ew_lsrk45_steps call)
-    and L2 errors against the analytic solution."""
+    T = 1, FP64, mixed and compensated: time of the whole run (one
+    ew_lsrk45_steps call) and L2 errors against the analytic solution."""
     import exwave_gb300 as ew
     amps, kvecs = [1.0, 0.5], [[1, 1], [2, 3]]
     m = ew.hypercube(2, 16, 0, 0.0, boundary_ids=2)
     dt = ew.time_step_size(m, 0.25 / 4 ** 1.5)
     steps = int(round(1.0 / dt))
     out, states = {}, {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "fp64", "mixed_ff"):
         op = ew.WaveEquationOperation(m, 4, precision=prec)
         stream = torch.cuda.current_stream()
         op.set_stream(stream)
@@ -400,11 +401,15 @@ def membrane2d(args, torch):
         states[prec] = (op, v)
     op64, v64 = states["fp64"]
     diff = op64.l2_difference(states["mixed"][1], v64)
+    diffc = op64.l2_difference(states["mixed_ff"][1], v64)
     return {"metric": "DoF-updates/s", "value": out["mixed"]["value"], "unit": "DoF-updates/s",
-            "mixed": out["mixed"], "fp64": out["fp64"],
+            "mixed": out["mixed"], "fp64": out["fp64"], "compensated": out["mixed_ff"],
             "error_ratio_p": out["mixed"]["l2_p"] / out["fp64"]["l2_p"],
             "error_ratio_u": out["mixed"]["l2_u"] / out["fp64"]["l2_u"],
+            "compensated_error_ratio_p": out["mixed_ff"]["l2_p"] / out["fp64"]["l2_p"],
+            "compensated_error_ratio_u": out["mixed_ff"]["l2_u"] / out["fp64"]["l2_u"],
             "mixed_vs_fp64_l2": {"p": diff[0], "u": diff[1]},
+            "compensated_vs_fp64_l2": {"p": diffc[0], "u": diffc[1]},
             "config": {"workload": "2-D vibrating membrane, 16^2 affine quads, FE_DGQ(4), LSRK45, "
                                    "512 steps to T=1", "n_dofs": op64.n_dofs, "dt": dt,
                        "steps": steps, "note": "launch-bound at this size (19,200 DoFs)"}}
@@ -498,7 +503,7 @@ def sweep_workload(args, torch):
     for k, n in ((2, 128), (3, 96), (4, 77), (5, 64), (6, 55), (7, 48)):
         m, dt = build_problem(n, k)
         row = {"degree": k, "cells": n}
-        for prec in ("mixed", "fp64"):
+        for prec in ("mixed", "fp64", "mixed_ff"):
             op = ew.WaveEquationOperation(m, k, precision=prec)
             steps = args.steps if prec == "mixed" else max(2, args.steps // 4)
             ms, _, errs, _ = time_steps(op, dt, steps, min(args.warmup, 3), torch, lambda: None)
@@ -507,6 +512,7 @@ def sweep_workload(args, torch):
                          "gbs": BYTES_PER_DOF_STEP[prec] * op.n_dofs / (ms / steps / 1e3) / 1e9}
             row["n_dofs"] = op.n_dofs
             op.close()
+        row["compensated_over_fp64"] = row["mixed_ff"]["value"] / row["fp64"]["value"]
         rows.append(row)
     return {"metric": "DoF-updates/s per degree", "rows": rows,
             "config": {"workload": "3-D membrane degree sweep at ~226M DoFs"}}
@@ -561,7 +567,8 @@ def main():
         "metric": "DoF-updates/s", "value": value, "unit": "DoF-updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32-operator/f64-state" if args.precision == "mixed" else "f64",
+        "dtype": {"mixed": "f32-operator/f64-state", "mixed_ff": "ff-operator/f32-input/f64-state",
+                  "fp64": "f64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": "3-D vibrating membrane, %d^3 affine hexes, FE_DGQ(%d), "
                                "LSRK45, %s" % (args.cells, args.degree, args.precision),
@@ -588,6 +595,18 @@ def main():
                           "error_ratio_p": errs[0] / errs64[0] if errs64[0] > 0 else None}
         op64.close()
         del op64
+        # the compensated operator: FP64-level error (see "errors") at FP32 data
+        opc = ew.WaveEquationOperation(m, args.degree, precision="mixed_ff", device=local)
+        stc = max(2, args.steps // 4)
+        msc, _, errsc, _ = time_steps(opc, dt, stc, 1, torch, barrier)
+        msc = rep.max(msc)
+        vc = n * STAGES * stc * ws / (msc / 1e3)
+        result["compensated"] = {"value": vc, "ms_per_step": msc / stc,
+                                 "errors": {"l2_p": errsc[0], "l2_u": errsc[1]},
+                                 "speedup_over_fp64": vc / v64,
+                                 "error_ratio_p_vs_fp64": errsc[0] / errs64[0] if errs64[0] > 0 else None}
+        opc.close()
+        del opc
     if not args.no_e2e:
         barrier()
         ms_e, h2d, d2h = e2e_steps(op, dt, args.steps, args.warmup, torch)

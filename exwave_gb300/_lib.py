@@ -14,6 +14,7 @@ STATUS = {0: "EW_OK", -1: "EW_ERR_INVALID", -2: "EW_ERR_UNSUPPORTED", -3: "EW_ER
           -4: "EW_ERR_OOM", -5: "EW_ERR_DEVICE", -6: "EW_ERR_TOO_LARGE"}
 EW_PREC_FP64 = 0
 EW_PREC_MIXED = 1
+EW_PREC_MIXED_FF = 2
 EW_MAX_DEGREE = 7
 
 # every entry point declared in include/exwave_gb300.h

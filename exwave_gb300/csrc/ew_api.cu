@@ -15,6 +15,7 @@
 
 #include "../../include/exwave_gb300.h"
 #include "ew_basis.h"
+#include "ew_ff.cuh"
 #include "ew_internal.h"
 #include "ew_launch.h"
 
@@ -549,6 +550,7 @@ struct ew_ctx {
   int dim = 0, degree = 0, np = 0, N = 0, F = 0;
   int64_t n_cells = 0, n_dofs = 0;
   bool mixed = false, cart = false, post = false;
+  bool ff = false;  // compensated operator (float-float arithmetic, FP32 data)
   int cb_stage = 1, cb_ck = 1;
   const ew::KernelTable* kt = nullptr;
   int32_t* d_nbr = nullptr;
@@ -784,6 +786,18 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
   a.single.bf = bf;
   a.single.mode = mode;
   cudaError_t e;
+  if (c->cart && c->ff) {
+    // compensated contexts: the float-float kernels of the same roles
+    switch (cvar) {
+      case ew::CV_MIX_APPLY64: cvar = ew::CV_FF_APPLY64; break;
+      case ew::CV_MIX_S1: cvar = ew::CV_FF_S1; break;
+      case ew::CV_MIX_MID: cvar = ew::CV_FF_MID; break;
+      case ew::CV_MIX_LAST: cvar = ew::CV_FF_LAST; break;
+      default:
+        return fail(c, EW_ERR_UNSUPPORTED,
+                    "this operation is not built for EW_PREC_MIXED_FF (apply and LSRK steps only)");
+    }
+  }
   if (c->cart) {
     // line kernel: stage X unless it is the accumulator itself (first LSRK
     // stage); bulk copies need 16-byte alignment
@@ -812,6 +826,7 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
 }
 
 int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
+  if (c->ff) return fail(c, EW_ERR_UNSUPPORTED, "ADER is not built for EW_PREC_MIXED_FF");
   ew::LaunchArgs a = base_args(c, true);
   a.single.X = src;
   a.single.Xout = T;
@@ -934,8 +949,13 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   std::memset(&opt, 0, sizeof(opt));
   opt.spectral_evaluation = 1;
   if (options) opt = *options;
-  if (opt.precision != EW_PREC_FP64 && opt.precision != EW_PREC_MIXED)
-    return fail(nullptr, EW_ERR_INVALID, "precision must be EW_PREC_FP64 or EW_PREC_MIXED");
+  if (opt.precision != EW_PREC_FP64 && opt.precision != EW_PREC_MIXED &&
+      opt.precision != EW_PREC_MIXED_FF)
+    return fail(nullptr, EW_ERR_INVALID,
+                "precision must be EW_PREC_FP64, EW_PREC_MIXED or EW_PREC_MIXED_FF");
+  if (opt.precision == EW_PREC_MIXED_FF && !cart)
+    return fail(nullptr, EW_ERR_UNSUPPORTED,
+                "EW_PREC_MIXED_FF (compensated operator) is built for axis-aligned cells only");
   if (!opt.spectral_evaluation)
     return fail(nullptr, EW_ERR_UNSUPPORTED,
                 "ADER with spectral_evaluation = false is not built (only the spectral "
@@ -962,7 +982,8 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   for (int d = 0; d < c->dim; ++d) c->N *= c->np;
   c->n_cells = mesh->n_cells;
   c->n_dofs = c->n_cells * c->F * c->N;
-  c->mixed = opt.precision == EW_PREC_MIXED;
+  c->mixed = opt.precision != EW_PREC_FP64;
+  c->ff = opt.precision == EW_PREC_MIXED_FF;
   c->cart = cart;
   c->post = opt.use_ader_post != 0;
   c->kt = &ew::kernel_table(c->dim, c->np);
@@ -1047,8 +1068,18 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       return bail(rc);
   }
   if (cart) {
-    if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_cellc), cellc.size() * rsz))) return bail(rc);
-    if (c->mixed) {
+    if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_cellc), cellc.size() * (c->ff ? 8 : rsz))))
+      return bail(rc);
+    if (c->ff) {
+      // each constant as a float pair (hi, lo)
+      std::vector<float> f(cellc.size() * 2);
+      for (size_t i = 0; i < cellc.size(); ++i) {
+        const ew::FF v = ew::FF::from_double(cellc[i]);
+        f[2 * i] = v.hi;
+        f[2 * i + 1] = v.lo;
+      }
+      rc = upload(c, c->d_cellc, f.data(), f.size() * 4);
+    } else if (c->mixed) {
       auto f = to_real_vec<float>(cellc);
       rc = upload(c, c->d_cellc, f.data(), f.size() * 4);
     } else {
@@ -1094,7 +1125,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block
                                          : (tuned > 0 ? tuned : std::max(1, 256 / lines));
     c->cb_cart = std::max(1, std::min(c->cb_cart, std::max(1, 512 / lines)));
-    const int v = c->mixed ? ew::CV_MIX_MID : ew::CV_F64_MID;
+    const int v = c->ff ? ew::CV_FF_MID : (c->mixed ? ew::CV_MIX_MID : ew::CV_F64_MID);
     while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1) > 110 * 1024) --c->cb_cart;
   }
   if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
@@ -1110,10 +1141,12 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     c->grid_ck = std::max(1, std::min(c->n_work_ck, std::max(occ, 1) * c->num_sms));
   }
   // integrator scratch: FP64 third register (also the ADER Taylor state);
-  // mixed: two FP32 stage inputs (the first also holds the ADER Taylor state)
+  // mixed: two FP32 stage inputs (the first also holds the ADER Taylor state);
+  // compensated: two stage inputs of float pairs
   if (c->mixed) {
-    if ((rc = dev_alloc(c, &c->d_x32[0], (size_t)c->n_dofs)) ||
-        (rc = dev_alloc(c, &c->d_x32[1], (size_t)c->n_dofs)))
+    const size_t per = c->ff ? 2 : 1;
+    if ((rc = dev_alloc(c, &c->d_x32[0], (size_t)c->n_dofs * per)) ||
+        (rc = dev_alloc(c, &c->d_x32[1], (size_t)c->n_dofs * per)))
       return bail(rc);
   } else {
     if ((rc = dev_alloc(c, &c->d_tmp64, (size_t)c->n_dofs))) return bail(rc);
@@ -1346,7 +1379,7 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
                ? EW_OK
                : fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
   using namespace ew;
-  if (!ctx->mixed || !ctx->cart) {
+  if (!ctx->mixed || !ctx->cart || ctx->ff) {
     // one step at a time; the state alternates between the two vectors
     double* a = vec_n;
     double* b = vec_np;
@@ -1434,6 +1467,10 @@ int ew_lsrk45_step_static(ew_ctx* ctx, double dt, double* vec_n, double* vec_np)
   if (rc) return rc;
   if (!vec_n || !vec_np || vec_n == vec_np)
     return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step_static: vec_n and vec_np must be distinct");
+  if (ctx->ff)
+    return fail(ctx, EW_ERR_UNSUPPORTED,
+                "ew_lsrk45_step_static: not built for EW_PREC_MIXED_FF (its stage inputs are float "
+                "pairs, twice the static scratch)");
   if (ctx->n_dofs > EW_STATIC_SCRATCH_MAX_DOFS)
     return fail(ctx, EW_ERR_TOO_LARGE,
                 "ew_lsrk45_step_static: " + std::to_string(ctx->n_dofs) +

@@ -24,9 +24,16 @@
 #include <cstring>
 #include <type_traits>
 
+#include "ew_ff.cuh"
 #include "ew_kernels.cuh"
 
 namespace ew {
+
+// compute types of the line arithmetic: FP64, FP32 or float-float (FF)
+template <typename R>
+constexpr bool is_f64_v = std::is_same<R, double>::value;
+template <typename R>
+constexpr bool is_ff_v = std::is_same<R, FF>::value;
 
 constexpr int ERR_WAIT_TIMEOUT = 8;
 
@@ -96,6 +103,7 @@ __device__ __forceinline__ void eo_apply(const EoMat<Real>& M, const Real* e, co
 namespace {
 __constant__ CartBasis<float> c_cart_f;
 __constant__ CartBasis<double> c_cart_d;
+__constant__ CartBasis<FF> c_cart_ff;
 }  // namespace
 template <typename Real>
 struct CartConst;
@@ -106,6 +114,10 @@ struct CartConst<float> {
 template <>
 struct CartConst<double> {
   static __device__ __forceinline__ const CartBasis<double>& get() { return c_cart_d; }
+};
+template <>
+struct CartConst<FF> {
+  static __device__ __forceinline__ const CartBasis<FF>& get() { return c_cart_ff; }
 };
 
 // Host: even-odd constants from the 1D Gauss data of NP points.
@@ -142,7 +154,12 @@ inline CartBasis<Real> cast_basis(const CartBasis<double>& d) {
   CartBasis<Real> r;
   const double* src = reinterpret_cast<const double*>(&d);
   Real* dst = reinterpret_cast<Real*>(&r);
-  for (size_t i = 0; i < sizeof(d) / sizeof(double); ++i) dst[i] = static_cast<Real>(src[i]);
+  for (size_t i = 0; i < sizeof(d) / sizeof(double); ++i) {
+    if constexpr (is_ff_v<Real>)
+      dst[i] = FF::from_double(src[i]);  // each constant as float + float remainder
+    else
+      dst[i] = static_cast<Real>(src[i]);
+  }
   return r;
 }
 
@@ -300,8 +317,10 @@ __device__ __forceinline__ float ff_lo(double d) { return __int_as_float(__doubl
 
 template <typename Real>
 __device__ __forceinline__ double real_to_f64(Real k) {
-  if constexpr (sizeof(Real) == 8)
+  if constexpr (is_f64_v<Real>)
     return k;
+  else if constexpr (is_ff_v<Real>)
+    return f32_to_f64(k.hi) + f32_to_f64(k.lo);
   else
     return f32_to_f64(k);
 }
@@ -312,7 +331,23 @@ template <int EPI, typename Real, typename OutT>
 __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k, OutT& xn,
                                           double& an) {
   xn = OutT(0);
-  if constexpr (EPI == EPI_APPLY) {
+  if constexpr (is_ff_v<Real>) {
+    // compensated operator: the update of the float-pair accumulator in FF
+    // arithmetic too (the mixed path rounds the increment to FP32)
+    static_assert(EPI == EPI_APPLY || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_LAST,
+                  "FF epilogues: apply, first, middle and last LSRK stage");
+    if constexpr (EPI == EPI_APPLY) {
+      an = real_to_f64<Real>(k);
+    } else if constexpr (EPI == EPI_MIX_LAST) {
+      const FF r = FF(ff_hi(a), ff_lo(a)) + FF(sd.f1_hi, sd.f1_lo) * k;
+      an = f32_to_f64(r.hi) + f32_to_f64(r.lo);
+    } else {
+      const FF acc(ff_hi(a), ff_lo(a));
+      xn = acc + FF(sd.f1_hi, sd.f1_lo) * k;
+      const FF r = acc + FF(sd.fb_hi, sd.fb_lo) * k;
+      an = ff_pack(r.hi, r.lo);
+    }
+  } else if constexpr (EPI == EPI_APPLY) {
     an = real_to_f64<Real>(k);
   } else if constexpr (EPI == EPI_F64_MID) {
     const double x = a + sd.f1 * k;
@@ -347,6 +382,9 @@ __device__ __forceinline__ void store2(float* p, float a, float b) {
 __device__ __forceinline__ void store2(double* p, double a, double b) {
   *reinterpret_cast<double2*>(p) = make_double2(a, b);
 }
+__device__ __forceinline__ void store2(FF* p, FF a, FF b) {
+  *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
+}
 
 struct CartArgs {
   LaunchArgs la;
@@ -355,15 +393,16 @@ struct CartArgs {
 };
 
 template <int DIM, int NP, typename Real, typename InT, int EPI>
-__global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) == 8) ? 80 : 72))
+__global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >= 7 || sizeof(InT) == 8) ? 80 : 72)))
     stage_cart_kernel(const CartArgs ca) {
-  using OutT = std::conditional_t<sizeof(Real) == 8, double, float>;
+  // next stage input: FP64, float pairs (compensated) or FP32
+  using OutT = std::conditional_t<is_f64_v<Real>, double, std::conditional_t<is_ff_v<Real>, FF, float>>;
   constexpr bool stage_a = EpiTraits<EPI>::stage_a;
   constexpr int N = ipow_c(NP, DIM);
   constexpr int F = DIM + 1;
   constexpr int NL = ipow_c(NP, DIM - 1);
   constexpr int H = NP / 2;
-  constexpr bool CONV = sizeof(Real) == 4 && sizeof(InT) == 8;
+  constexpr bool CONV = !is_f64_v<Real> && is_f64_v<InT>;
   constexpr bool LO_IN = EpiTraits<EPI>::lo_in;
   constexpr bool LO_OUT = EpiTraits<EPI>::lo_out;
   constexpr int A_ELEM = EpiTraits<EPI>::a_elem;
@@ -567,7 +606,16 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
       }
       if (stage_x) {
         double* sX64 = reinterpret_cast<double*>(sX);
-        for (int i = threadIdx.x; i < tot; i += blockDim.x) sX64[i] = ff_pack(f64_to_f32(sX64[i]), 0.f);
+        if constexpr (is_ff_v<Real>) {
+          // compensated operator: the exact pair of each value
+          for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+            float hi, lo;
+            f64_split(sX64[i], hi, lo);
+            sX64[i] = ff_pack(hi, lo);
+          }
+        } else {
+          for (int i = threadIdx.x; i < tot; i += blockDim.x) sX64[i] = ff_pack(f64_to_f32(sX64[i]), 0.f);
+        }
       }
       // these generic writes precede the bulk copy that refills the buffer
       fence_proxy_async();
@@ -577,8 +625,12 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
     // ---------------------------------------------------------- line phase
     // stage input values as Real, from the X buffer or (X == A) the A buffer
     auto xval = [&](int idx) -> Real {
-      if constexpr (sizeof(InT) == 4) {
+      if constexpr (sizeof(InT) == 4 || is_ff_v<InT>) {
         return sX[idx];
+      } else if constexpr (CONV && is_ff_v<Real>) {
+        const float* p = reinterpret_cast<const float*>(stage_x ? static_cast<const void*>(sX)
+                                                                : static_cast<const void*>(sA));
+        return Real(p[2 * idx], p[2 * idx + 1]);
       } else if constexpr (CONV) {
         return reinterpret_cast<const float*>(stage_x ? static_cast<const void*>(sX)
                                                       : static_cast<const void*>(sA))[2 * idx];
@@ -704,7 +756,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 96 : ((NP >= 7 || sizeof(InT) ==
         if (a_ok) {
           const bool paired = NP % 2 == 0 && e == 0 &&
                               (reinterpret_cast<uintptr_t>(sd.Aout) & 15) == 0 &&
-                              (reinterpret_cast<uintptr_t>(sd.Xout) & 7) == 0;
+                              (reinterpret_cast<uintptr_t>(sd.Xout) & (2 * sizeof(OutT) - 1)) == 0;
 #pragma unroll
           for (int i = 0; i < NP; i += 2) {
             OutT x0, x1 = OutT(0);

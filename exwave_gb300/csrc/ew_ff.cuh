@@ -1,0 +1,83 @@
+// ew_ff.cuh -- float-float arithmetic for the compensated operator.
+//
+// An FF value is the unevaluated sum hi + lo of two floats.  Products use the
+// exact FMA residual of hi*hi (Dekker's product with a fused multiply-add),
+// sums use Knuth's error-free two-sum; results are renormalised with a fast
+// two-sum so that |lo| <= ulp(hi)/2.  About 44 significant bits: enough that
+// the rounding of the operator's sums and coefficients no longer shows in
+// the discretisation error, while the data stay FP32.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ew_device.cuh"
+
+namespace ew {
+
+struct FF {
+  float hi, lo;
+  FF() = default;
+  __host__ __device__ constexpr FF(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr FF(float v) : hi(v), lo(0.f) {}
+  // split of a double into its nearest float and the float nearest the rest
+  __host__ __device__ static FF from_double(double d) {
+    const float h = (float)d;
+    return FF(h, (float)(d - (double)h));
+  }
+  __host__ __device__ double to_double() const { return (double)hi + (double)lo; }
+};
+
+// s + e = a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+}
+
+// s + e = a + b exactly, for |a| >= |b| (or a == 0)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ FF operator+(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  FF r;
+  fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ FF operator-(FF a) { return FF(-a.hi, -a.lo); }
+__device__ __forceinline__ FF operator-(FF a, FF b) { return a + (-b); }
+
+__device__ __forceinline__ FF operator*(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  FF r;
+  fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ FF operator*(FF a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  float e = __fmaf_rn(a.hi, b, -p);
+  e = __fmaf_rn(a.lo, b, e);
+  FF r;
+  fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ FF operator*(float a, FF b) { return b * a; }
+__device__ __forceinline__ FF& operator+=(FF& a, FF b) { return a = a + b; }
+__device__ __forceinline__ FF& operator-=(FF& a, FF b) { return a = a - b; }
+__device__ __forceinline__ FF& operator*=(FF& a, FF b) { return a = a * b; }
+
+// read-only load of a pair (8-byte aligned: arrays of FF)
+template <>
+__device__ __forceinline__ FF load_nc<FF>(const FF* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return FF(v.x, v.y);
+}
+
+}  // namespace ew

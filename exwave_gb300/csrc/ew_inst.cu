@@ -134,7 +134,10 @@ cudaError_t set_constants(const double* w, const double* D, const double* L0, co
   const CartBasis<float> cf = cast_basis<float>(cd);
   cudaError_t e = cudaMemcpyToSymbol(c_cart_d, &cd, sizeof(cd));
   if (e != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(c_cart_f, &cf, sizeof(cf));
+  e = cudaMemcpyToSymbol(c_cart_f, &cf, sizeof(cf));
+  if (e != cudaSuccess) return e;
+  const CartBasis<FF> cff = cast_basis<FF>(cd);
+  return cudaMemcpyToSymbol(c_cart_ff, &cff, sizeof(cff));
 }
 
 template <class K>
@@ -167,6 +170,10 @@ void EW_TABLE_FN(KernelTable& t) {
   fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
   fill_cart<CartK<float, float, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
   fill_cart<CartK<float, float, EPI_MIX_LAST_FF>>(t.cart[CV_MIX_LAST_FF]);
+  fill_cart<CartK<FF, double, EPI_APPLY>>(t.cart[CV_FF_APPLY64]);
+  fill_cart<CartK<FF, double, EPI_MIX_S1>>(t.cart[CV_FF_S1]);
+  fill_cart<CartK<FF, FF, EPI_MIX_MID>>(t.cart[CV_FF_MID]);
+  fill_cart<CartK<FF, FF, EPI_MIX_LAST>>(t.cart[CV_FF_LAST]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);

@@ -20,6 +20,8 @@
 // vector is streamed from HBM about once per stage.
 #pragma once
 
+#include <type_traits>
+
 #include "ew_device.cuh"
 
 namespace ew {
@@ -74,8 +76,19 @@ struct CkSmem {
 
 template <typename Real, typename T>
 __device__ __forceinline__ Real to_real(T v) {
-  if constexpr (sizeof(Real) == 4 && sizeof(T) == 8) {
+  if constexpr (std::is_same<Real, T>::value) {
+    return v;
+  } else if constexpr (sizeof(Real) == 4 && sizeof(T) == 8) {
     return f64_to_f32(v);
+  } else if constexpr (sizeof(Real) == 8 && !std::is_floating_point<Real>::value) {
+    // float-float from FP64: the exact pair; from FP32: the value
+    if constexpr (std::is_same<T, double>::value) {
+      float hi, lo;
+      f64_split(v, hi, lo);
+      return Real(hi, lo);
+    } else {
+      return Real(v);
+    }
   } else {
     return static_cast<Real>(v);
   }

@@ -36,7 +36,11 @@ enum CartVariant : int {
   CV_MIX_UPD = 8,     // mixed ADER update u + M^-1 A(T)
   CV_MIX_S1_FF = 9,   // mixed stage 1, state held as float pairs (multi-step calls)
   CV_MIX_LAST_FF = 10,  // mixed stage 5, state left as float pairs
-  N_CART_VARIANTS = 11
+  CV_FF_APPLY64 = 11,   // compensated (float-float) operator on an FP64 input
+  CV_FF_S1 = 12,        // compensated LSRK stage 1 (FP64 state in)
+  CV_FF_MID = 13,       // compensated LSRK stages 2..4 (float-pair stage inputs)
+  CV_FF_LAST = 14,      // compensated LSRK stage 5 (FP64 state out)
+  N_CART_VARIANTS = 15
 };
 
 // Launcher of the Cartesian line kernel.

@@ -9,7 +9,8 @@ import numpy as np
 
 from . import _lib
 
-PRECISIONS = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED}
+PRECISIONS = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED,
+              "mixed_ff": _lib.EW_PREC_MIXED_FF}
 
 
 def _ptr(t):

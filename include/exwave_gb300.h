@@ -43,8 +43,14 @@ typedef enum ew_status {
 } ew_status;
 
 typedef enum ew_precision {
-  EW_PREC_FP64 = 0, /* operator, geometry and state in FP64 */
-  EW_PREC_MIXED = 1 /* operator and geometry in FP32, state/accumulation FP64 */
+  EW_PREC_FP64 = 0,     /* operator, geometry and state in FP64 */
+  EW_PREC_MIXED = 1,    /* operator and geometry in FP32, state/accumulation FP64 */
+  EW_PREC_MIXED_FF = 2  /* compensated: FP32 stage inputs, the operator's arithmetic and
+                           coefficients in float-float (about 44 bits), state FP64.
+                           Axis-aligned cells; apply and the LSRK steps
+                           (ew_apply, ew_lsrk45_step(s), ew_lsrk_step,
+                           ew_aderadconfull_step); ADER and batches return
+                           EW_ERR_UNSUPPORTED */
 } ew_precision;
 
 typedef enum ew_boundary {

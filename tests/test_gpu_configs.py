@@ -106,3 +106,21 @@ def test_receivers_match_oracle(env, dim, k, n):
     np.testing.assert_allclose(got[:, dim].cpu().numpy(), ref, rtol=1e-12, atol=1e-12)
     with pytest.raises(Exception):
         op.set_receivers(np.full((1, dim), 1.5))
+
+
+@pytest.mark.parametrize("k", [2, 3, 4])
+def test_membrane2d_compensated_error(env, k):
+    """The compensated operator (EW_PREC_MIXED_FF: float-pair data,
+    float-float arithmetic and coefficients): after the 2560 stages to T = 1
+    the state equals the FP64 path's to 1e-12 (L2), so the L2 errors match
+    within 1.1x (in fact to 1e-6 relative) for k = 2, 3 and 4 (the
+    configuration; the mixed path's k = 4 error is 3.5x the FP64 one)."""
+    ew, oracle, torch, _ = env
+    op64, v64, t = run_degree(ew, torch, k, "fp64")
+    opc, vc, _ = run_degree(ew, torch, k, "mixed_ff")
+    e64 = op64.l2_errors(v64, AMPS, KVECS, t)
+    ec = opc.l2_errors(vc, AMPS, KVECS, t)
+    diff = op64.l2_difference(vc, v64)
+    assert ec[0] <= 1.1 * e64[0] and ec[1] <= 1.1 * e64[1], (ec, e64)
+    assert abs(ec[0] - e64[0]) <= 1e-6 * e64[0] and abs(ec[1] - e64[1]) <= 1e-6 * e64[1]
+    assert diff[0] < 1e-12 and diff[1] < 1e-12, diff

@@ -255,3 +255,48 @@ def test_ragged_work_lists_and_single_cells(env, case, precision):
     op.synchronize()
     err = np.abs(vnp.cpu().numpy() - a).max() / np.abs(a).max()
     assert err < tol, ("lsrk45", err)
+
+
+@pytest.mark.parametrize("case", [CASES[i] for i in (0, 1, 3, 6, 8, 11)], ids=ids)
+def test_compensated_apply_and_steps(env, case):
+    """EW_PREC_MIXED_FF on axis-aligned meshes (FP64 inputs split exactly into
+    float pairs, stage inputs kept as float pairs, the operator's arithmetic
+    and coefficients in float-float): apply and three LSRK45 steps equal the
+    FP64 oracle to 1e-12 relative, the FP64 path's own bound."""
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=k + 10 * dim)
+    op = ew.WaveEquationOperation(m, k, precision="mixed_ff")
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    rng = np.random.default_rng(99 + k)
+    u = rng.standard_normal(o.n_dofs)
+    ref_out = o.apply(u)
+    src = torch.from_numpy(u).cuda()
+    dst = torch.zeros_like(src)
+    op.apply(src, dst)
+    op.synchronize()
+    err = np.abs(dst.cpu().numpy() - ref_out).max() / np.abs(ref_out).max()
+    assert err < FP64_TOL, err
+    u0 = o.project_reference(2)
+    dt = o.time_step(0.2 / k ** 1.5)
+    a, b = u0.copy(), np.zeros_like(u0)
+    for _ in range(3):
+        o.lsrk45_step(dt, a, b)
+        a, b = b, a
+    vn = torch.from_numpy(u0.copy()).cuda()
+    vnp = torch.zeros_like(vn)
+    op.lsrk45_steps(dt, 3, vn, vnp)
+    op.synchronize()
+    err = np.abs(vnp.cpu().numpy() - a).max() / np.abs(a).max()
+    assert err < FP64_TOL, err
+
+
+def test_compensated_rejects_curved_and_ader(env):
+    ew, oracle, torch = env
+    from exwave_gb300 import _lib
+    with pytest.raises(_lib.EwError):
+        ew.WaveEquationOperation(ew.hypercube(2, 3, 0, 0.1), 2, precision="mixed_ff")
+    op = ew.WaveEquationOperation(ew.hypercube(2, 3, 0, 0.0), 2, precision="mixed_ff")
+    a, b = op.new_vector(), op.new_vector()
+    with pytest.raises(_lib.EwError):
+        op.ader_step(0.01, a, b)
