@@ -38,7 +38,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 STAGES = 5
-BYTES_PER_DOF_STEP = {"mixed": 112.0, "mixed_ff": 112.0, "fp64": 144.0}
+# algorithmic bytes per DoF and LSRK45 step: each vector once per stage at
+# its stored precision (mixed: FP32 stage inputs; compensated: float pairs)
+BYTES_PER_DOF_STEP = {"mixed": 112.0, "mixed_ff": 144.0, "fp64": 144.0}
 
 
 def parse():
