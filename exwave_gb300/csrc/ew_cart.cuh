@@ -37,6 +37,23 @@ constexpr bool is_ff_v = std::is_same<R, FF>::value;
 
 constexpr int ERR_WAIT_TIMEOUT = 8;
 
+// acc + a * b in a chain of sums, and the end of the chain (float-float:
+// fused, with one renormalisation at the end; FP32 / FP64: a fused multiply-add)
+template <typename R>
+__device__ __forceinline__ R mac(R acc, R a, R b) {
+  if constexpr (std::is_same<R, FF>::value)
+    return ff_mac(acc, a, b);
+  else
+    return acc + a * b;
+}
+template <typename R>
+__device__ __forceinline__ R end_sum(R v) {
+  if constexpr (std::is_same<R, FF>::value)
+    return ff_norm(v);
+  else
+    return v;
+}
+
 // Even-odd form of an NP x NP matrix M with M[n-1-i][n-1-j] = -M[i][j]:
 // for i < H = NP/2, a_i = sum_j P_ij e_j (+ mid_col_i x_m), b_i = sum_j Q_ij o_j,
 // y_i = a_i + b_i, y_{n-1-i} = b_i - a_i, and for odd NP y_m = sum_j mid_row_j o_j,
@@ -83,18 +100,18 @@ __device__ __forceinline__ void eo_apply(const EoMat<Real>& M, const Real* e, co
     Real s = Real(0), t = Real(0);
 #pragma unroll
     for (int j = 0; j < H; ++j) {
-      s += M.P[i][j] * e[j];
-      t += M.Q[i][j] * o[j];
+      s = mac(s, M.P[i][j], e[j]);
+      t = mac(t, M.Q[i][j], o[j]);
     }
-    if constexpr (NP % 2 == 1) s += M.mid_col[i] * xm;
-    a[i] = s;
-    b[i] = t;
+    if constexpr (NP % 2 == 1) s = mac(s, M.mid_col[i], xm);
+    a[i] = end_sum(s);
+    b[i] = end_sum(t);
   }
   if constexpr (NP % 2 == 1) {
     Real s = Real(0);
 #pragma unroll
-    for (int j = 0; j < H; ++j) s += M.mid_row[j] * o[j];
-    a[H] = s;  // middle output (no pair)
+    for (int j = 0; j < H; ++j) s = mac(s, M.mid_row[j], o[j]);
+    a[H] = end_sum(s);  // middle output (no pair)
   }
 }
 
@@ -667,11 +684,15 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
         Real sp = (NP % 2) ? B.Lmid * pm : Real(0), ap = Real(0);
 #pragma unroll
         for (int j = 0; j < H; ++j) {
-          su += B.Ls[j] * eu[j];
-          au += B.La[j] * ou[j];
-          sp += B.Ls[j] * ep[j];
-          ap += B.La[j] * op[j];
+          su = mac(su, B.Ls[j], eu[j]);
+          au = mac(au, B.La[j], ou[j]);
+          sp = mac(sp, B.Ls[j], ep[j]);
+          ap = mac(ap, B.La[j], op[j]);
         }
+        su = end_sum(su);
+        au = end_sum(au);
+        sp = end_sum(sp);
+        ap = end_sum(ap);
         const Real tu[2] = {su + au, su - au};
         const Real tp[2] = {sp + ap, sp - ap};
         cp_async_wait_all();  // this thread's neighbour lines
@@ -691,8 +712,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
 #pragma unroll
               for (int j = 0; j < NP; ++j) {
                 const Real l = B.L[1 - s][j];
-                vu += l * to_real<Real>(nslot[((2 * s) * NP + j) * nstride]);
-                vp += l * to_real<Real>(nslot[((2 * s + 1) * NP + j) * nstride]);
+                vu = mac(vu, l, to_real<Real>(nslot[((2 * s) * NP + j) * nstride]));
+                vp = mac(vp, l, to_real<Real>(nslot[((2 * s + 1) * NP + j) * nstride]));
               }
             } else {
               // neighbour in this block: its trace on the opposite face, l_j(1-s)
@@ -700,10 +721,12 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
 #pragma unroll
               for (int j = 0; j < NP; ++j) {
                 const Real l = B.L[1 - s][j];
-                vu += l * xval(no + e * N + base + j * str);
-                vp += l * xval(no + DIM * N + base + j * str);
+                vu = mac(vu, l, xval(no + e * N + base + j * str));
+                vp = mac(vp, l, xval(no + DIM * N + base + j * str));
               }
             }
+            vu = end_sum(vu);
+            vp = end_sum(vp);
             const Real tau_m = cst[7 + 2 * (2 * e + s)];
             const Real tau_inv = cst[8 + 2 * (2 * e + s)];
             const Real un_m = -nrm * vu;

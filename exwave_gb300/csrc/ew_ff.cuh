@@ -73,6 +73,24 @@ __device__ __forceinline__ FF& operator+=(FF& a, FF b) { return a = a + b; }
 __device__ __forceinline__ FF& operator-=(FF& a, FF b) { return a = a - b; }
 __device__ __forceinline__ FF& operator*=(FF& a, FF b) { return a = a * b; }
 
+// acc + a * b inside a sum: one exact product and one two-sum, the result
+// left unnormalised (its lo part collects the errors of the chain, which
+// ff_norm folds in once at the end)
+__device__ __forceinline__ FF ff_mac(FF acc, FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  float s, t;
+  two_sum(acc.hi, p, s, t);
+  return FF(s, __fadd_rn(t, __fadd_rn(acc.lo, e)));
+}
+__device__ __forceinline__ FF ff_norm(FF v) {
+  FF r;
+  two_sum(v.hi, v.lo, r.hi, r.lo);
+  return r;
+}
+
 // read-only load of a pair (8-byte aligned: arrays of FF)
 template <>
 __device__ __forceinline__ FF load_nc<FF>(const FF* p) {
