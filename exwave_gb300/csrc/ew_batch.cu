@@ -547,6 +547,7 @@ extern "C" {
 int ew_batch_create(const ew_batch_options* opt, ew_batch** out) {
   if (!opt || !out) return EW_ERR_INVALID;
   *out = nullptr;
+  if (opt->precision == EW_PREC_MIXED_FF) return EW_ERR_UNSUPPORTED;  // compensated: single solves only
   if (opt->precision != EW_PREC_FP64 && opt->precision != EW_PREC_MIXED) return EW_ERR_INVALID;
   if (opt->hbm_budget_bytes <= 0 || opt->max_solves <= 0) return EW_ERR_INVALID;
   int ndev = 0;

@@ -300,3 +300,5 @@ def test_compensated_rejects_curved_and_ader(env):
     a, b = op.new_vector(), op.new_vector()
     with pytest.raises(_lib.EwError):
         op.ader_step(0.01, a, b)
+    from exwave_gb300.operator import _ptr
+    assert op.L.ew_lsrk45_step_static(op.ctx, 0.01, _ptr(a), _ptr(b)) == -2  # EW_ERR_UNSUPPORTED
