@@ -19,6 +19,11 @@
 // refilled at the start of each item, which keeps the block small enough
 // for four resident blocks per SM.  Waits are bounded; on time-out the
 // kernel raises ERR_WAIT_TIMEOUT and stops.
+//
+// Compute types: FP64 (the reference's arithmetic), FP32 (mixed precision)
+// or FF, an unevaluated float pair (ew_ff.cuh) for the compensated
+// precision: stage inputs, constants and every sum and product of the line
+// work in float-float, about 44 significant bits on the FP32 pipes.
 #pragma once
 
 #include <cstring>
