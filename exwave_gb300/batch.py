@@ -109,7 +109,8 @@ class Batch:
                  use_graphs=True, device=0):
         self.L = _L()
         o = BatchOptions()
-        o.precision = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED}[precision]
+        o.precision = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED,
+                       "mixed_ff": _lib.EW_PREC_MIXED_FF}[precision]
         o.device = device
         o.hbm_budget_bytes = int(hbm_budget_bytes)
         o.max_solves = max_solves

@@ -31,6 +31,7 @@
 #include "../../include/exwave_gb300.h"
 #include "ew_basis.h"
 #include "ew_device.cuh"
+#include "ew_ff.cuh"
 #include "ew_internal.h"
 
 namespace {
@@ -191,7 +192,8 @@ std::vector<T> cast_vec(const std::vector<double>& v) {
 
 struct ew_batch {
   int device = 0;
-  bool mixed = true;
+  bool mixed = true;  // FP32 or float-float operator (else FP64)
+  bool ff = false;    // compensated: float-float operator, FP64 state between steps
   bool use_graphs = true;
   int num_sms = 0;
   int max_solves = 0;
@@ -243,11 +245,13 @@ struct Layout {
   size_t U, X, nbr, cellc, src_w, rec_w, rec_cell, trace, clock, total;
 };
 
-Layout solve_layout(const ew_solve_desc* s, bool mixed) {
+// precision: 0 FP64, 1 mixed (FP32 data), 2 compensated (float pairs)
+Layout solve_layout(const ew_solve_desc* s, int precision) {
   const int dim = s->mesh.dim, np = s->mesh.degree + 1;
   int N = 1;
   for (int d = 0; d < dim; ++d) N *= np;
   const int64_t n_dofs = s->mesh.n_cells * (dim + 1) * N;
+  const bool mixed = precision == 1;
   const size_t rsz = mixed ? 4 : 8;
   auto al = [](size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); };
   Layout L;
@@ -255,7 +259,7 @@ Layout solve_layout(const ew_solve_desc* s, bool mixed) {
   L.U = o;
   o += 2 * al((size_t)n_dofs * 8);
   L.X = o;
-  o += mixed ? 2 * al((size_t)n_dofs * 4) : al((size_t)n_dofs * 8);
+  o += mixed ? 2 * al((size_t)n_dofs * 4) : (precision == 2 ? 2 * al((size_t)n_dofs * 8) : al((size_t)n_dofs * 8));
   L.nbr = o;
   o += al((size_t)s->mesh.n_cells * 2 * dim * 4);
   L.cellc = o;
@@ -326,7 +330,19 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
   const double* A[5];
   void* Xo[5];
   double* Ao[5];
-  if (b->mixed) {
+  if (b->ff) {
+    // compensated: FP64 state in U[parity] read by the first stage (X == A),
+    // float-pair accumulator in U[1 - parity], float-pair stage inputs
+    // alternating in X[0] / X[1]; the last stage leaves the FP64 state in
+    // U[1 - parity]
+    void* Y0 = s.X[0];
+    void* Y1 = s.X[1];
+    X[0] = Nv; A[0] = Nv; Xo[0] = Y0; Ao[0] = Pv;
+    X[1] = Y0; A[1] = Pv; Xo[1] = Y1; Ao[1] = Pv;
+    X[2] = Y1; A[2] = Pv; Xo[2] = Y0; Ao[2] = Pv;
+    X[3] = Y0; A[3] = Pv; Xo[3] = Y1; Ao[3] = Pv;
+    X[4] = Y1; A[4] = Pv; Xo[4] = nullptr; Ao[4] = Pv;
+  } else if (b->mixed) {
     // state pair: hi in X[parity], lo in U[1] (floats); accumulator in U[0];
     // the last stage leaves the new hi in X[1 - parity] and lo in U[1]
     void* Xh = s.X[parity];
@@ -392,14 +408,17 @@ int rebuild(ew_batch* b) {
     g.members = kv.second;
     const ew::KernelTable& kt = ew::kernel_table(g.dim, g.np);
     const int lines = kt.lines;
-    const int tuned = ew::tuned_cells_per_block(g.dim, g.np - 1, b->mixed ? 1 : 0);
+    const int tuned = b->ff ? 0 : ew::tuned_cells_per_block(g.dim, g.np - 1, b->mixed ? 1 : 0);
     g.cb = tuned > 0 ? std::min(tuned, std::max(1, 512 / lines)) : std::max(1, 256 / lines);
     const int NP = g.np;
     int N = 1;
     for (int d = 0; d < g.dim; ++d) N *= NP;
     const int F = g.dim + 1;
     for (int st = 0; st < 5; ++st) {
-      if (b->mixed) {
+      if (b->ff) {
+        g.variant[st] = st == 0 ? ew::CV_FF_S1 : (st < 4 ? ew::CV_FF_MID : ew::CV_FF_LAST);
+        g.sx[st] = (st == 0) ? 0 : 1;  // first stage: X is the FP64 state (the accumulator)
+      } else if (b->mixed) {
         g.variant[st] = st == 0 ? ew::CV_MIX_S1_FF : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST_FF);
         g.sx[st] = 1;
       } else {
@@ -408,7 +427,7 @@ int rebuild(ew_batch* b) {
       }
     }
     while (g.cb > 1 && kt.cart[g.variant[1]].smem(g.cb, 1) > 110 * 1024) --g.cb;
-    const size_t cell_x = (size_t)F * N * (b->mixed ? 4 : 8);
+    const size_t cell_x = (size_t)F * N * (b->mixed && !b->ff ? 4 : 8);
     g.tma = (cell_x % 16 == 0) && (((size_t)F * N * 8) % 16 == 0);
     // tables
     const size_t nslot = g.members.size();
@@ -461,7 +480,7 @@ int rebuild(ew_batch* b) {
       r.H[0] = static_cast<const float*>(s.X[0]);
       r.H[1] = static_cast<const float*>(s.X[1]);
       r.L = reinterpret_cast<const float*>(s.U[1]);
-      r.mixed = b->mixed ? 1 : 0;
+      r.mixed = b->mixed && !b->ff ? 1 : 0;  // float-pair state between steps
       r.pad = 0;
       r.rec_w = s.rec_w;
       r.rec_cell = s.rec_cell;
@@ -547,15 +566,17 @@ extern "C" {
 int ew_batch_create(const ew_batch_options* opt, ew_batch** out) {
   if (!opt || !out) return EW_ERR_INVALID;
   *out = nullptr;
-  if (opt->precision == EW_PREC_MIXED_FF) return EW_ERR_UNSUPPORTED;  // compensated: single solves only
-  if (opt->precision != EW_PREC_FP64 && opt->precision != EW_PREC_MIXED) return EW_ERR_INVALID;
+  if (opt->precision != EW_PREC_FP64 && opt->precision != EW_PREC_MIXED &&
+      opt->precision != EW_PREC_MIXED_FF)
+    return EW_ERR_INVALID;
   if (opt->hbm_budget_bytes <= 0 || opt->max_solves <= 0) return EW_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || opt->device < 0 || opt->device >= ndev)
     return EW_ERR_CUDA;
   ew_batch* b = new ew_batch;
   b->device = opt->device;
-  b->mixed = opt->precision == EW_PREC_MIXED;
+  b->mixed = opt->precision != EW_PREC_FP64;
+  b->ff = opt->precision == EW_PREC_MIXED_FF;
   b->use_graphs = opt->use_graphs != 0;
   b->max_solves = opt->max_solves;
   cudaSetDevice(b->device);
@@ -595,7 +616,7 @@ int64_t ew_batch_solve_bytes(const ew_batch* b, const ew_solve_desc* s) {
   if (!b || !s || s->mesh.n_cells <= 0 || s->mesh.degree < 1 || s->mesh.degree > EW_MAX_DEGREE ||
       (s->mesh.dim != 2 && s->mesh.dim != 3))
     return -1;
-  return (int64_t)solve_layout(s, b->mixed).total;
+  return (int64_t)solve_layout(s, b->ff ? 2 : (b->mixed ? 1 : 0)).total;
 }
 
 int64_t ew_batch_bytes_free(const ew_batch* b) { return b ? (int64_t)b->arena.free_bytes() : -1; }
@@ -613,7 +634,7 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
     return bfail(b, EW_ERR_INVALID, "0..1 sources and 0..64 receivers");
   if ((int)b->solves.size() >= b->max_solves) return bfail(b, EW_ERR_TOO_LARGE, "max_solves reached");
   cudaSetDevice(b->device);
-  const Layout L = solve_layout(sd, b->mixed);
+  const Layout L = solve_layout(sd, b->ff ? 2 : (b->mixed ? 1 : 0));
   size_t off = 0;
   if (!b->arena.alloc(L.total, &off)) return bfail(b, EW_ERR_OOM, "HBM budget exhausted");
   Solve s;
@@ -635,7 +656,7 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   s.U[0] = reinterpret_cast<double*>(base + L.U);
   s.U[1] = reinterpret_cast<double*>(base + L.U + ud);
   if (b->mixed) {
-    const size_t xd = ((size_t)s.n_dofs * 4 + kAlign - 1) & ~(kAlign - 1);
+    const size_t xd = ((size_t)s.n_dofs * (b->ff ? 8 : 4) + kAlign - 1) & ~(kAlign - 1);
     s.X[0] = base + L.X;
     s.X[1] = base + L.X + xd;
   } else {
@@ -718,7 +739,22 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
     if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->stream);
   };
   std::vector<float> cf, sf;
-  if (b->mixed) {
+  if (b->ff) {
+    // float pairs (hi, lo) of the FP64 values
+    auto pairs = [](const std::vector<double>& v) {
+      std::vector<float> r(v.size() * 2);
+      for (size_t i = 0; i < v.size(); ++i) {
+        const ew::FF f = ew::FF::from_double(v[i]);
+        r[2 * i] = f.hi;
+        r[2 * i + 1] = f.lo;
+      }
+      return r;
+    };
+    cf = pairs(cellc);
+    sf = pairs(srcw);
+    up(s.cellc, cf.data(), cf.size() * 4);
+    up(s.src_w, sf.data(), sf.size() * 4);
+  } else if (b->mixed) {
     cf = cast_vec<float>(cellc);
     sf = cast_vec<float>(srcw);
     up(s.cellc, cf.data(), cf.size() * 4);
@@ -733,7 +769,7 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   if (e == cudaSuccess) e = cudaMemsetAsync(s.U[0], 0, (size_t)s.n_dofs * 8, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.U[1], 0, (size_t)s.n_dofs * 8, b->stream);
   // mixed: the zero state's hi and lo parts
-  for (int k = 0; b->mixed && k < 2; ++k)
+  for (int k = 0; b->mixed && !b->ff && k < 2; ++k)
     if (e == cudaSuccess) e = cudaMemsetAsync(s.X[k], 0, (size_t)s.n_dofs * 4, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.clock, 0, 16, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // host vectors go out of scope
@@ -766,7 +802,7 @@ int ew_batch_set_state(ew_batch* b, int32_t id, const double* state) {
   cudaSetDevice(b->device);
   if (s->steps_done != 0) return bfail(b, EW_ERR_INVALID, "set_state before the first step only");
   cudaError_t e;
-  if (b->mixed) {
+  if (b->mixed && !b->ff) {
     // the state's hi and lo parts, read by the next first stage
     const int threads = 256;
     const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
@@ -786,7 +822,7 @@ int ew_batch_get_state(ew_batch* b, int32_t id, double* state) {
   if (!s) return bfail(b, EW_ERR_INVALID, "unknown solve id");
   cudaSetDevice(b->device);
   cudaError_t e;
-  if (b->mixed) {
+  if (b->mixed && !b->ff) {
     const int threads = 256;
     const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
     join_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(

@@ -809,8 +809,13 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     // ---------------------------------------------------------- pressure
     const int src_local = sd.src_cell - wi.cell_begin;
     Real src_val = Real(0);
-    if (src_local >= 0 && src_local < nc)
-      src_val = static_cast<Real>(sd.src_amp * ricker(*sd.time + sd.c_stage * sd.dt, sd.src_f0, sd.src_t0));
+    if (src_local >= 0 && src_local < nc) {
+      const double sv = sd.src_amp * ricker(*sd.time + sd.c_stage * sd.dt, sd.src_f0, sd.src_t0);
+      if constexpr (is_ff_v<Real>)
+        src_val = FF::from_double(sv);
+      else
+        src_val = static_cast<Real>(sv);
+    }
     wait_a();
     for (int idx = threadIdx.x; a_ok && idx < nc * N; idx += blockDim.x) {
       const int cl = idx / N;

@@ -45,12 +45,13 @@ typedef enum ew_status {
 typedef enum ew_precision {
   EW_PREC_FP64 = 0,     /* operator, geometry and state in FP64 */
   EW_PREC_MIXED = 1,    /* operator and geometry in FP32, state/accumulation FP64 */
-  EW_PREC_MIXED_FF = 2  /* compensated: FP32 stage inputs, the operator's arithmetic and
-                           coefficients in float-float (about 44 bits), state FP64.
-                           Axis-aligned cells; apply and the LSRK steps
+  EW_PREC_MIXED_FF = 2  /* compensated: stage inputs as float pairs, the operator's
+                           arithmetic and coefficients in float-float (about 44
+                           bits), state FP64; equal to the FP64 path to about
+                           1e-14.  Axis-aligned cells; apply, the LSRK steps
                            (ew_apply, ew_lsrk45_step(s), ew_lsrk_step,
-                           ew_aderadconfull_step); ADER and batches return
-                           EW_ERR_UNSUPPORTED */
+                           ew_aderadconfull_step) and batches; ADER and the
+                           static step return EW_ERR_UNSUPPORTED */
 } ew_precision;
 
 typedef enum ew_boundary {

@@ -30,12 +30,15 @@ RECEIVERS = np.array([[0.31, 0.52, 0.47], [0.73, 0.21, 0.66], [0.5, 0.5, 0.9]])
 SOURCE = ([0.43, 0.57, 0.38], 6.0, 1.0 / 6.0 * 0.2, 3.0)
 
 
-def test_source_and_receivers_match_oracle(env):
+@pytest.mark.parametrize("precision", ["fp64", "mixed_ff"])
+def test_source_and_receivers_match_oracle(env, precision):
+    """FP64 and compensated batches with a Ricker source and receivers
+    against the oracle: state to 1e-12, receiver traces to 1e-11."""
     ew, batch, oracle, torch = env
     m = hetero_mesh(ew, 5, 3)
     k = 3
     dt = ew.time_step_size(m, 0.25 / k ** 1.5)
-    b = batch.Batch(precision="fp64", hbm_budget_bytes=1 << 30)
+    b = batch.Batch(precision=precision, hbm_budget_bytes=1 << 30)
     sid = b.add(batch.Solve(m, k, dt, 12, source=SOURCE, receivers=RECEIVERS))
     o = oracle.Problem.from_mesh(3, k, m.vertices, m.neighbors, m.speed, m.density)
     u, v = o.zeros(), o.zeros()
@@ -88,7 +91,7 @@ def test_alone_equals_mixed_batch(env):
     assert np.array_equal(mix.receivers(ib), ref_rec)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_ff"])
 def test_batch_matches_single_context(env, precision):
     ew, batch, oracle, torch = env
     m = ew.hypercube(3, 5)
@@ -107,7 +110,8 @@ def test_batch_matches_single_context(env, precision):
     op.synchronize()
     b.synchronize()
     got = b.get_state(sid, torch.zeros_like(u0))
-    if precision == "fp64":
+    if precision in ("fp64", "mixed_ff"):
+        # the same kernels on the same FP64 state between steps: bit-identical
         assert torch.equal(got, vn)
     else:
         # the batch carries the state's FP32 split between steps and runs
