@@ -225,17 +225,19 @@ EDGE = [
 
 
 @pytest.mark.parametrize("case", EDGE, ids=lambda c: "d%dk%d_n%d_f%g_cb%d" % (c[0], c[1], c[2], c[3], c[5]))
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_ff"])
 def test_ragged_work_lists_and_single_cells(env, case, precision):
     """Meshes of one cell (all faces on the boundary) and work lists whose
     last item is only partly filled: apply and three LSRK45 steps against
     the oracle."""
     ew, oracle, torch = env
     dim, k, n, f, bids, cb = case
+    if precision == "mixed_ff" and f != 0.0 and n > 1:
+        pytest.skip("the compensated operator is built for axis-aligned cells")
     m = ew.hypercube(dim, n, 0, f, boundary_ids=bids)
     op = ew.WaveEquationOperation(m, k, precision=precision, cells_per_block=cb)
     o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
-    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    tol = MIXED_TOL if precision == "mixed" else FP64_TOL
     rng = np.random.default_rng(77 + k)
     u = rng.standard_normal(o.n_dofs)
     ref_out = o.apply(u)
