@@ -394,8 +394,11 @@ __global__ void __launch_bounds__(1024) post_pressure_kernel(const double* verts
   double* g = z + Mp;            // dim x Mp
   double* red = g + 3 * Mp;      // 33
   const double* V = verts + c * (1 << dim) * dim;
-  const double rho_c = mat_fp64 ? static_cast<const double*>(mat)[4 * c]
-                                 : (double)static_cast<const float*>(mat)[4 * c];
+  // materials: 0 FP32, 1 FP64, 2 float pairs
+  const double rho_c = mat_fp64 == 1   ? static_cast<const double*>(mat)[4 * c]
+                       : mat_fp64 == 2 ? (double)static_cast<const float*>(mat)[8 * c] +
+                                             (double)static_cast<const float*>(mat)[8 * c + 1]
+                                       : (double)static_cast<const float*>(mat)[4 * c];
   int ii[3] = {0, 0, 0};
   {
     int q = i;
@@ -786,17 +789,19 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
   a.single.bf = bf;
   a.single.mode = mode;
   cudaError_t e;
-  if (c->cart && c->ff) {
+  if (c->ff) {
     // compensated contexts: the float-float kernels of the same roles
     switch (cvar) {
       case ew::CV_MIX_APPLY64: cvar = ew::CV_FF_APPLY64; break;
       case ew::CV_MIX_S1: cvar = ew::CV_FF_S1; break;
       case ew::CV_MIX_MID: cvar = ew::CV_FF_MID; break;
       case ew::CV_MIX_LAST: cvar = ew::CV_FF_LAST; break;
+      case ew::CV_MIX_UPD: cvar = ew::CV_FF_UPD; break;
+      case ew::CV_MIX_APPLY32: cvar = ew::CV_FF_APPLYFF; break;
       default:
-        return fail(c, EW_ERR_UNSUPPORTED,
-                    "this operation is not built for EW_PREC_MIXED_FF (apply and LSRK steps only)");
+        return fail(c, EW_ERR_UNSUPPORTED, "this operation is not built for EW_PREC_MIXED_FF");
     }
+    variant = variant == ew::STAGE_MIX_IN64 ? ew::STAGE_FF_IN64 : ew::STAGE_FF_INFF;
   }
   if (c->cart) {
     // line kernel: stage X unless it is the accumulator itself (first LSRK
@@ -826,7 +831,6 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
 }
 
 int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
-  if (c->ff) return fail(c, EW_ERR_UNSUPPORTED, "ADER is not built for EW_PREC_MIXED_FF");
   ew::LaunchArgs a = base_args(c, true);
   a.single.X = src;
   a.single.Xout = T;
@@ -845,7 +849,7 @@ int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
     a.ck_fac[s] = (float)(fac * dtp);
     dtp *= dt;
   }
-  const ew::KernelEntry& k = c->kt->ck[c->mixed ? 1 : 0][c->cart ? 1 : 0][c->post ? 1 : 0];
+  const ew::KernelEntry& k = c->kt->ck[c->ff ? 2 : (c->mixed ? 1 : 0)][c->cart ? 1 : 0][c->post ? 1 : 0];
   cudaError_t e = k.launch(a, c->grid_ck, c->stream);
   ++c->launches;
   if (e != cudaSuccess) return cuda_fail(c, e, "ck kernel launch");
@@ -953,9 +957,6 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       opt.precision != EW_PREC_MIXED_FF)
     return fail(nullptr, EW_ERR_INVALID,
                 "precision must be EW_PREC_FP64, EW_PREC_MIXED or EW_PREC_MIXED_FF");
-  if (opt.precision == EW_PREC_MIXED_FF && !cart)
-    return fail(nullptr, EW_ERR_UNSUPPORTED,
-                "EW_PREC_MIXED_FF (compensated operator) is built for axis-aligned cells only");
   if (!opt.spectral_evaluation)
     return fail(nullptr, EW_ERR_UNSUPPORTED,
                 "ADER with spectral_evaluation = false is not built (only the spectral "
@@ -1046,7 +1047,8 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       }
     }
   }
-  const size_t rsz = c->mixed ? sizeof(float) : sizeof(double);
+  // geometry, materials and basis in the compute type: FP64, FP32 or float pairs
+  const size_t rsz = c->mixed && !c->ff ? sizeof(float) : sizeof(double);
   if ((rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_geo), geo.size() * rsz)) ||
       (rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_mat), mat.size() * rsz)) ||
       (rc = dev_alloc(c, reinterpret_cast<char**>(&c->d_basis), basis.size() * rsz)) ||
@@ -1055,7 +1057,22 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       (rc = dev_alloc(c, &c->d_nodes, (size_t)c->np)) || (rc = dev_alloc(c, &c->d_err, 4)) ||
       (rc = dev_alloc(c, &c->d_acc, 4)))
     return bail(rc);
-  if (c->mixed) {
+  if (c->ff) {
+    auto pairs = [](const std::vector<double>& v) {
+      std::vector<float> r(v.size() * 2);
+      for (size_t i = 0; i < v.size(); ++i) {
+        const ew::FF f = ew::FF::from_double(v[i]);
+        r[2 * i] = f.hi;
+        r[2 * i + 1] = f.lo;
+      }
+      return r;
+    };
+    auto g = pairs(geo), m = pairs(mat), b = pairs(basis);
+    if ((rc = upload(c, c->d_geo, g.data(), g.size() * 4)) ||
+        (rc = upload(c, c->d_mat, m.data(), m.size() * 4)) ||
+        (rc = upload(c, c->d_basis, b.data(), b.size() * 4)))
+      return bail(rc);
+  } else if (c->mixed) {
     auto g = to_real_vec<float>(geo), m = to_real_vec<float>(mat), b = to_real_vec<float>(basis);
     if ((rc = upload(c, c->d_geo, g.data(), g.size() * 4)) ||
         (rc = upload(c, c->d_mat, m.data(), m.size() * 4)) ||
@@ -1114,8 +1131,8 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   // work lists and persistent grid sizes
   c->cb_stage = default_cb(c->N, opt.cells_per_block);
   // mixed CK kernel: 80 registers a thread, two blocks per SM need 384 threads or fewer
-  c->cb_ck = c->mixed ? std::max(1, std::min(c->cb_stage, 384 / c->N)) : c->cb_stage;
-  const int ck_var = c->mixed ? 1 : 0;
+  c->cb_ck = c->mixed && !c->ff ? std::max(1, std::min(c->cb_stage, 384 / c->N)) : c->cb_stage;
+  const int ck_var = c->ff ? 2 : (c->mixed ? 1 : 0);
   while (c->cb_ck > 1 &&
          c->kt->ck[ck_var][cart][c->post].smem(c->cb_ck) > 200 * 1024)
     --c->cb_ck;
@@ -1133,6 +1150,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       (cart && (rc = build_work(c, c->cb_cart, &c->d_work_cart, &c->n_work_cart))))
     return bail(rc);
   for (int v = 0; v < ew::N_STAGE_VARIANTS; ++v) {
+    if (!c->kt->stage[v][cart].occupancy) continue;  // compensated variants: curved cells only
     const int occ = c->kt->stage[v][cart].occupancy(c->cb_stage);
     c->grid_stage[v] = std::max(1, std::min(c->n_work_stage, std::max(occ, 1) * c->num_sms));
   }
@@ -1802,7 +1820,7 @@ int ew_l2_error_post_membrane(ew_ctx* ctx, const double* state, int32_t n_modes,
                                 (int)smem)) != cudaSuccess)
     return cuda_fail(ctx, e, "post kernel attribute");
   ew::post_pressure_kernel<<<(unsigned)ctx->n_cells, (Mp + 31) / 32 * 32, smem, ctx->stream>>>(
-      ctx->d_verts, ctx->d_mat, ctx->mixed ? 0 : 1, dim, np, ctx->d_post, state, ctx->d_ad[0], ms, t,
+      ctx->d_verts, ctx->d_mat, ctx->ff ? 2 : (ctx->mixed ? 0 : 1), dim, np, ctx->d_post, state, ctx->d_ad[0], ms, t,
       ctx->d_acc);
   ++ctx->launches;
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "post kernel launch");

@@ -34,12 +34,6 @@
 
 namespace ew {
 
-// compute types of the line arithmetic: FP64, FP32 or float-float (FF)
-template <typename R>
-constexpr bool is_f64_v = std::is_same<R, double>::value;
-template <typename R>
-constexpr bool is_ff_v = std::is_same<R, FF>::value;
-
 constexpr int ERR_WAIT_TIMEOUT = 8;
 
 // acc + a * b in a chain of sums, and the end of the chain (float-float:
@@ -356,10 +350,15 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
   if constexpr (is_ff_v<Real>) {
     // compensated operator: the update of the float-pair accumulator in FF
     // arithmetic too (the mixed path rounds the increment to FP32)
-    static_assert(EPI == EPI_APPLY || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_LAST,
-                  "FF epilogues: apply, first, middle and last LSRK stage");
+    static_assert(EPI == EPI_APPLY || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_LAST ||
+                      EPI == EPI_MIX_UPD,
+                  "FF epilogues: apply, LSRK stages 1, middle and 5, ADER update");
     if constexpr (EPI == EPI_APPLY) {
       an = real_to_f64<Real>(k);
+    } else if constexpr (EPI == EPI_MIX_UPD) {
+      // ADER update u + M^-1 A(T): the FF increment rounded once to FP64
+      const FF inc = FF(sd.f1_hi, sd.f1_lo) * k;
+      an = a + (f32_to_f64(inc.hi) + f32_to_f64(inc.lo));
     } else if constexpr (EPI == EPI_MIX_LAST) {
       const FF r = FF(ff_hi(a), ff_lo(a)) + FF(sd.f1_hi, sd.f1_lo) * k;
       an = f32_to_f64(r.hi) + f32_to_f64(r.lo);

@@ -10,9 +10,18 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "ew_device.cuh"
 
 namespace ew {
+
+struct FF;
+// compute types of the operator arithmetic: FP64, FP32 or float-float (FF)
+template <typename R>
+constexpr bool is_f64_v = std::is_same<R, double>::value;
+template <typename R>
+constexpr bool is_ff_v = std::is_same<R, FF>::value;
 
 struct FF {
   float hi, lo;
@@ -72,6 +81,48 @@ __device__ __forceinline__ FF operator*(float a, FF b) { return b * a; }
 __device__ __forceinline__ FF& operator+=(FF& a, FF b) { return a = a + b; }
 __device__ __forceinline__ FF& operator-=(FF& a, FF b) { return a = a - b; }
 __device__ __forceinline__ FF& operator*=(FF& a, FF b) { return a = a * b; }
+
+// a / b by long division: quotient digits a.hi / b.hi, each followed by the
+// exact remainder in float-float (about 44 bits)
+__device__ __forceinline__ FF operator/(FF a, FF b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const FF r1 = a - b * q1;
+  const float q2 = __fdiv_rn(r1.hi, b.hi);
+  const FF r2 = r1 - b * q2;
+  const float q3 = __fdiv_rn(r2.hi, b.hi);
+  FF q;
+  fast_two_sum(q1, q2, q.hi, q.lo);
+  return q + FF(q3);
+}
+__device__ __forceinline__ FF& operator/=(FF& a, FF b) { return a = a / b; }
+
+// square root: the float root and one Newton correction from the exact
+// residual (a >= 0)
+__device__ __forceinline__ FF ff_sqrt(FF a) {
+  if (!(a.hi > 0.f)) return FF(0.f);
+  const float s = __fsqrt_rn(a.hi);
+  const FF r = a - FF(s) * FF(s);
+  FF q;
+  fast_two_sum(s, __fdiv_rn(r.hi, 2.f * s), q.hi, q.lo);
+  return q;
+}
+__device__ __forceinline__ FF ff_fabs(FF a) { return a.hi < 0.f ? -a : a; }
+
+// square root and absolute value in the compute type
+template <typename R>
+__device__ __forceinline__ R real_sqrt(R v) {
+  if constexpr (is_ff_v<R>)
+    return ff_sqrt(v);
+  else
+    return sqrt(v);
+}
+template <typename R>
+__device__ __forceinline__ R real_fabs(R v) {
+  if constexpr (is_ff_v<R>)
+    return ff_fabs(v);
+  else
+    return fabs(v);
+}
 
 // acc + a * b inside a sum: one exact product and one two-sum, the result
 // left unnormalised (its lo part collects the errors of the chain, which

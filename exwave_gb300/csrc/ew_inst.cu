@@ -174,6 +174,8 @@ void EW_TABLE_FN(KernelTable& t) {
   fill_cart<CartK<FF, double, EPI_MIX_S1>>(t.cart[CV_FF_S1]);
   fill_cart<CartK<FF, FF, EPI_MIX_MID>>(t.cart[CV_FF_MID]);
   fill_cart<CartK<FF, FF, EPI_MIX_LAST>>(t.cart[CV_FF_LAST]);
+  fill_cart<CartK<FF, FF, EPI_MIX_UPD>>(t.cart[CV_FF_UPD]);
+  fill_cart<CartK<FF, FF, EPI_APPLY>>(t.cart[CV_FF_APPLYFF]);
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);
@@ -181,6 +183,9 @@ void EW_TABLE_FN(KernelTable& t) {
   fill<StageK<float, double, float, true>>(t.stage[STAGE_MIX_IN64][1]);
   fill<StageK<float, float, float, false>>(t.stage[STAGE_MIX_IN32][0]);
   fill<StageK<float, float, float, true>>(t.stage[STAGE_MIX_IN32][1]);
+  // compensated: curved cells only (axis-aligned cells use the line kernel)
+  fill<StageK<FF, double, FF, false>>(t.stage[STAGE_FF_IN64][0]);
+  fill<StageK<FF, FF, FF, false>>(t.stage[STAGE_FF_INFF][0]);
   // CK kernels: [precision][cart][post]
   fill<CkK<double, double, double, false, false>>(t.ck[0][0][0]);
   fill<CkK<double, double, double, false, true>>(t.ck[0][0][1]);
@@ -190,6 +195,10 @@ void EW_TABLE_FN(KernelTable& t) {
   fill<CkK<float, double, float, false, true>>(t.ck[1][0][1]);
   fill<CkK<float, double, float, true, false>>(t.ck[1][1][0]);
   fill<CkK<float, double, float, true, true>>(t.ck[1][1][1]);
+  fill<CkK<FF, double, FF, false, false>>(t.ck[2][0][0]);
+  fill<CkK<FF, double, FF, false, true>>(t.ck[2][0][1]);
+  fill<CkK<FF, double, FF, true, false>>(t.ck[2][1][0]);
+  fill<CkK<FF, double, FF, true, true>>(t.ck[2][1][1]);
 }
 
 }  // namespace ew

@@ -22,7 +22,7 @@
 
 #include <type_traits>
 
-#include "ew_device.cuh"
+#include "ew_ff.cuh"
 
 namespace ew {
 
@@ -232,11 +232,11 @@ __device__ __forceinline__ void op_face(const Real* sB, const Real* sX, Real* sF
       nrm[d] = sgn * JiT[d][e];
       len2 += nrm[d] * nrm[d];
     }
-    const Real len = sqrt(len2);
+    const Real len = real_sqrt(len2);
     const Real il = Real(1) / len;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) nrm[d] *= il;
-    jxw_f = wt * fabs(det) * len;
+    jxw_f = wt * real_fabs(det) * len;
   }
   const Real rho = sMat[4 * cl], c = sMat[4 * cl + 1];
   const Real rho_inv = Real(1) / rho, c_sq = c * c;
@@ -418,10 +418,28 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
     if (mode == MODE_APPLY) {
 #pragma unroll
       for (int fld = 0; fld < F; ++fld) {
-        if constexpr (sizeof(Real) == 8)
+        if constexpr (is_f64_v<Real>)
           sd.Aout[g0 + fld * N] = k[fld];
+        else if constexpr (is_ff_v<Real>)
+          sd.Aout[g0 + fld * N] = f32_to_f64(k[fld].hi) + f32_to_f64(k[fld].lo);
         else
           sd.Aout[g0 + fld * N] = f32_to_f64(k[fld]);
+      }
+    } else if constexpr (is_ff_v<Real>) {
+      // compensated: next stage input a + f1 k as a float pair, FP64
+      // accumulator a + (f1 + f2) k (or a + f1 k) from the FF increment
+      const bool mid = mode == MODE_RK_MID;
+#pragma unroll
+      for (int fld = 0; fld < F; ++fld) {
+        const size_t g = g0 + fld * N;
+        const double a = sd.A[g];
+        if (mid) {
+          float ah, al;
+          f64_split(a, ah, al);
+          static_cast<FF*>(sd.Xout)[g] = FF(ah, al) + FF(sd.f1_hi, sd.f1_lo) * k[fld];
+        }
+        const FF inc = (mid ? FF(sd.fb_hi, sd.fb_lo) : FF(sd.f1_hi, sd.f1_lo)) * k[fld];
+        sd.Aout[g] = a + (f32_to_f64(inc.hi) + f32_to_f64(inc.lo));
       }
     } else {
       // one FP64 operation per value whatever the mode (a data-independent
@@ -431,7 +449,7 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
       for (int fld = 0; fld < F; ++fld) {
         const size_t g = g0 + fld * N;
         const double a = sd.A[g];
-        if constexpr (sizeof(Real) == 8) {
+        if constexpr (is_f64_v<Real>) {
           const double xn = a + sd.f1 * k[fld];
           if (mid) static_cast<OutT*>(sd.Xout)[g] = static_cast<OutT>(xn);
           sd.Aout[g] = fma(mid ? sd.f2 : 0.0, k[fld], xn);
@@ -666,15 +684,20 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
   Real fac[8];
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
-    if constexpr (sizeof(Real) == 8)
+    if constexpr (is_f64_v<Real>)
       fac[s] = La.ck_fac_d[s];
+    else if constexpr (is_ff_v<Real>)
+      fac[s] = FF::from_double(La.ck_fac_d[s]);
     else
       fac[s] = La.ck_fac[s];
   }
   Real dtr, half_dt2;
-  if constexpr (sizeof(Real) == 8) {
+  if constexpr (is_f64_v<Real>) {
     dtr = La.ck_dt_d;
     half_dt2 = La.ck_half_dt2_d;
+  } else if constexpr (is_ff_v<Real>) {
+    dtr = FF::from_double(La.ck_dt_d);
+    half_dt2 = FF::from_double(La.ck_half_dt2_d);
   } else {
     dtr = La.ck_dt;
     half_dt2 = La.ck_half_dt2;

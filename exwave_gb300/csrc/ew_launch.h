@@ -13,7 +13,9 @@ enum StageVariant : int {
   STAGE_F64 = 0,       // FP64 operator, FP64 input and output
   STAGE_MIX_IN64 = 1,  // FP32 operator reading an FP64 input (first stage, apply)
   STAGE_MIX_IN32 = 2,  // FP32 operator reading an FP32 stage input
-  N_STAGE_VARIANTS = 3
+  STAGE_FF_IN64 = 3,   // float-float operator reading an FP64 input (curved cells only)
+  STAGE_FF_INFF = 4,   // float-float operator reading a float-pair stage input (curved cells only)
+  N_STAGE_VARIANTS = 5
 };
 
 struct KernelEntry {
@@ -40,7 +42,9 @@ enum CartVariant : int {
   CV_FF_S1 = 12,        // compensated LSRK stage 1 (FP64 state in)
   CV_FF_MID = 13,       // compensated LSRK stages 2..4 (float-pair stage inputs)
   CV_FF_LAST = 14,      // compensated LSRK stage 5 (FP64 state out)
-  N_CART_VARIANTS = 15
+  CV_FF_UPD = 15,       // compensated ADER update u + M^-1 A(T), T as float pairs
+  CV_FF_APPLYFF = 16,   // compensated operator on a float-pair input
+  N_CART_VARIANTS = 17
 };
 
 // Launcher of the Cartesian line kernel.
@@ -55,7 +59,7 @@ struct KernelTable {
   int lines = 0;  // threads per cell of the Cartesian kernel: dim * np^(dim-1)
   KernelEntry stage[N_STAGE_VARIANTS][2];  // [variant][cartesian]
   CartEntry cart[N_CART_VARIANTS];
-  KernelEntry ck[2][2][2];                 // [mixed][cartesian][post]
+  KernelEntry ck[3][2][2];                 // [FP64 / mixed / compensated][cartesian][post]
   // upload the even-odd 1D constants of this degree to the current device
   cudaError_t (*set_constants)(const double* w, const double* D, const double* L0,
                                const double* L1) = nullptr;

@@ -103,11 +103,11 @@ __device__ __forceinline__ void op_face_staged(const Real* sB, const Real* sX, R
     nrm[d] = sgn * JiT[d][e];
     len2 += nrm[d] * nrm[d];
   }
-  const Real len = sqrt(len2);
+  const Real len = real_sqrt(len2);
   const Real il = Real(1) / len;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) nrm[d] *= il;
-  const Real jxw_f = wt * fabs(det) * len;
+  const Real jxw_f = wt * real_fabs(det) * len;
   const Real rho = sMat[4 * cl], c = sMat[4 * cl + 1];
   const Real rho_inv = Real(1) / rho, c_sq = c * c;
   const Real tau_p = Real(1) / (c * rho);
@@ -279,10 +279,28 @@ __global__ void __launch_bounds__(512, sizeof(Real) == 4 ? 2 : 1) stage_kernel_s
       if (!stage_a) {
 #pragma unroll
         for (int fld = 0; fld < F; ++fld) {
-          if constexpr (sizeof(Real) == 8)
+          if constexpr (is_f64_v<Real>)
             sd.Aout[g0 + fld * N] = k[fld];
+          else if constexpr (is_ff_v<Real>)
+            sd.Aout[g0 + fld * N] = f32_to_f64(k[fld].hi) + f32_to_f64(k[fld].lo);
           else
             sd.Aout[g0 + fld * N] = f32_to_f64(k[fld]);
+        }
+      } else if constexpr (is_ff_v<Real>) {
+        // compensated: next stage input a + f1 k as a float pair, FP64
+        // accumulator from the FF increment
+        const bool mid = sd.mode == MODE_RK_MID;
+#pragma unroll
+        for (int fld = 0; fld < F; ++fld) {
+          const size_t g = g0 + fld * N;
+          const double a = sA[l0 + fld * N];
+          if (mid) {
+            float ah, al;
+            f64_split(a, ah, al);
+            static_cast<FF*>(sd.Xout)[g] = FF(ah, al) + FF(sd.f1_hi, sd.f1_lo) * k[fld];
+          }
+          const FF inc = (mid ? FF(sd.fb_hi, sd.fb_lo) : FF(sd.f1_hi, sd.f1_lo)) * k[fld];
+          sd.Aout[g] = a + (f32_to_f64(inc.hi) + f32_to_f64(inc.lo));
         }
       } else {
         // stage_kernel's epilogue with the staged accumulator
@@ -291,7 +309,7 @@ __global__ void __launch_bounds__(512, sizeof(Real) == 4 ? 2 : 1) stage_kernel_s
         for (int fld = 0; fld < F; ++fld) {
           const size_t g = g0 + fld * N;
           const double a = sA[l0 + fld * N];
-          if constexpr (sizeof(Real) == 8) {
+          if constexpr (is_f64_v<Real>) {
             const double xn = a + sd.f1 * k[fld];
             if (mid) static_cast<OutT*>(sd.Xout)[g] = static_cast<OutT>(xn);
             sd.Aout[g] = fma(mid ? sd.f2 : 0.0, k[fld], xn);

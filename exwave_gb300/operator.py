@@ -34,8 +34,8 @@ class WaveEquationOperation:
 
     precision: "fp64" (the reference's arithmetic), "mixed" (FP32 operator,
     FP64 state) or "mixed_ff" (compensated: float-float operator on
-    float-pair data, equal to the FP64 path to about 1e-14; axis-aligned
-    meshes and the RK integrators only)."""
+    float-pair data, equal to the FP64 path to about 1e-14; every mesh and
+    integrator, ADER included)."""
 
     def __init__(self, mesh, degree, precision="fp64", use_ader_post=False, cells_per_block=0,
                  device=0):

@@ -48,10 +48,9 @@ typedef enum ew_precision {
   EW_PREC_MIXED_FF = 2  /* compensated: stage inputs as float pairs, the operator's
                            arithmetic and coefficients in float-float (about 44
                            bits), state FP64; equal to the FP64 path to about
-                           1e-14.  Axis-aligned cells; apply, the LSRK steps
-                           (ew_apply, ew_lsrk45_step(s), ew_lsrk_step,
-                           ew_aderadconfull_step) and batches; ADER and the
-                           static step return EW_ERR_UNSUPPORTED */
+                           1e-14.  Axis-aligned and curved cells, every
+                           integrator, ADER and batches; the static step
+                           (ew_lsrk45_step_static) returns EW_ERR_UNSUPPORTED */
 } ew_precision;
 
 typedef enum ew_boundary {

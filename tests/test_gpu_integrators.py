@@ -35,8 +35,6 @@ def env(oracle_mod):
 def test_integrator_matches_oracle(env, name, precision, case):
     ew, driver, oracle, torch = env
     dim, k, n, ref, f, bids, het = case
-    if precision == "mixed_ff" and f != 0.0:
-        pytest.skip("the compensated operator is built for axis-aligned cells")
     m = ew.hypercube(dim, n, ref, f, boundary_ids=bids)
     if het:
         rng = np.random.default_rng(5)
@@ -59,7 +57,10 @@ def test_integrator_matches_oracle(env, name, precision, case):
         vn, vnp = vnp, vn
     op.synchronize()
     err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
-    assert err < (1e-5 if precision == "mixed" else 1e-12), err
+    # compensated (float-float, about 44 bits): FP64's bound on axis-aligned
+    # cells, 1e-11 where the curved-cell metric terms enter
+    tol = {"fp64": 1e-12, "mixed": 1e-5, "mixed_ff": 1e-12 if f == 0.0 else 1e-11}[precision]
+    assert err < tol, err
 
 
 def test_lsrk_step_rejects_unknown_scheme(env):

@@ -3,7 +3,10 @@ oracle on the same meshes and seeded inputs.
 
 Tolerances: FP64 path 1e-12 relative to the largest entry (round-off of
 reordered sums); mixed path (FP32 operator, FP64 state) 2e-5 relative for a
-single operator application."""
+single operator application; compensated path (float-float operator, FP64
+state) 1e-12 on axis-aligned cells and 1e-11 where curved-cell metric terms or
+the ADER derivative chain enter (float-float carries about 44 bits, a unit
+round-off near 500 times FP64's)."""
 import numpy as np
 import pytest
 
@@ -11,6 +14,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
 MIXED_TOL = 2e-5
+FF_TOL = 1e-11
 
 
 @pytest.fixture(scope="module")
@@ -140,11 +144,14 @@ def test_lsrk45_steps_call(env, case, precision, n_steps):
 
 @pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 5, 9, 10, 13)], ids=ids)
 @pytest.mark.parametrize("post", [False, True])
-def test_ader_step(env, case, post):
+@pytest.mark.parametrize("precision", ["fp64", "mixed_ff"])
+def test_ader_step(env, case, post, precision):
+    """apply_ader and two ADER steps (± post) against the oracle, on the FP64
+    (1e-12 relative) and the compensated float-float path (1e-11 relative)."""
     ew, oracle, torch = env
     dim, k, n, ref, f, bids, het = case
     m = make_case(ew, dim, n, ref, f, bids, het, seed=11)
-    op = ew.WaveEquationOperation(m, k, precision="fp64", use_ader_post=post)
+    op = ew.WaveEquationOperation(m, k, precision=precision, use_ader_post=post)
     o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
     o.set_ader_post(post)
     u0 = o.project_reference(2)
@@ -155,8 +162,9 @@ def test_ader_step(env, case, post):
     dst = torch.zeros_like(src)
     op.apply_ader(src, dst, dt)
     op.synchronize()
+    tol = FP64_TOL if precision == "fp64" else FF_TOL
     err = np.abs(dst.cpu().numpy() - ref_dst).max() / np.abs(ref_dst).max()
-    assert err < FP64_TOL, err
+    assert err < tol, err
     # two full steps
     a, b = u0.copy(), np.zeros_like(u0)
     vn = torch.from_numpy(u0.copy()).cuda()
@@ -168,7 +176,7 @@ def test_ader_step(env, case, post):
         vn, vnp = vnp, vn
     op.synchronize()
     err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
-    assert err < FP64_TOL, err
+    assert err < tol, err
 
 
 def test_rk_update_matches_reference_updater(env):
@@ -232,12 +240,11 @@ def test_ragged_work_lists_and_single_cells(env, case, precision):
     the oracle."""
     ew, oracle, torch = env
     dim, k, n, f, bids, cb = case
-    if precision == "mixed_ff" and f != 0.0 and n > 1:
-        pytest.skip("the compensated operator is built for axis-aligned cells")
     m = ew.hypercube(dim, n, 0, f, boundary_ids=bids)
     op = ew.WaveEquationOperation(m, k, precision=precision, cells_per_block=cb)
     o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
-    tol = MIXED_TOL if precision == "mixed" else FP64_TOL
+    tol = {"fp64": FP64_TOL, "mixed": MIXED_TOL,
+           "mixed_ff": FP64_TOL if f == 0.0 else FF_TOL}[precision]
     rng = np.random.default_rng(77 + k)
     u = rng.standard_normal(o.n_dofs)
     ref_out = o.apply(u)
@@ -259,12 +266,13 @@ def test_ragged_work_lists_and_single_cells(env, case, precision):
     assert err < tol, ("lsrk45", err)
 
 
-@pytest.mark.parametrize("case", [CASES[i] for i in (0, 1, 3, 6, 8, 11)], ids=ids)
+@pytest.mark.parametrize("case", [CASES[i] for i in (0, 1, 2, 3, 5, 6, 8, 9, 10, 11)], ids=ids)
 def test_compensated_apply_and_steps(env, case):
-    """EW_PREC_MIXED_FF on axis-aligned meshes (FP64 inputs split exactly into
+    """EW_PREC_MIXED_FF on axis-aligned and curved meshes (FP64 inputs split exactly into
     float pairs, stage inputs kept as float pairs, the operator's arithmetic
     and coefficients in float-float): apply and three LSRK45 steps equal the
-    FP64 oracle to 1e-12 relative, the FP64 path's own bound."""
+    FP64 oracle to 1e-12 relative on axis-aligned cells, the FP64 path's own
+    bound, and to 1e-11 on curved cells."""
     ew, oracle, torch = env
     dim, k, n, ref, f, bids, het = case
     m = make_case(ew, dim, n, ref, f, bids, het, seed=k + 10 * dim)
@@ -277,8 +285,9 @@ def test_compensated_apply_and_steps(env, case):
     dst = torch.zeros_like(src)
     op.apply(src, dst)
     op.synchronize()
+    tol = FP64_TOL if f == 0.0 else FF_TOL
     err = np.abs(dst.cpu().numpy() - ref_out).max() / np.abs(ref_out).max()
-    assert err < FP64_TOL, err
+    assert err < tol, err
     u0 = o.project_reference(2)
     dt = o.time_step(0.2 / k ** 1.5)
     a, b = u0.copy(), np.zeros_like(u0)
@@ -290,17 +299,12 @@ def test_compensated_apply_and_steps(env, case):
     op.lsrk45_steps(dt, 3, vn, vnp)
     op.synchronize()
     err = np.abs(vnp.cpu().numpy() - a).max() / np.abs(a).max()
-    assert err < FP64_TOL, err
+    assert err < tol, err
 
 
-def test_compensated_rejects_curved_and_ader(env):
+def test_compensated_rejects_static_step(env):
     ew, oracle, torch = env
-    from exwave_gb300 import _lib
-    with pytest.raises(_lib.EwError):
-        ew.WaveEquationOperation(ew.hypercube(2, 3, 0, 0.1), 2, precision="mixed_ff")
     op = ew.WaveEquationOperation(ew.hypercube(2, 3, 0, 0.0), 2, precision="mixed_ff")
     a, b = op.new_vector(), op.new_vector()
-    with pytest.raises(_lib.EwError):
-        op.ader_step(0.01, a, b)
     from exwave_gb300.operator import _ptr
     assert op.L.ew_lsrk45_step_static(op.ctx, 0.01, _ptr(a), _ptr(b)) == -2  # EW_ERR_UNSUPPORTED

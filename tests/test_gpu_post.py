@@ -49,16 +49,14 @@ def test_post_error_matches_oracle(env, case):
     ref = o.post_error_reference(a, 2, t)
     amps, kv = ew.reference_mode(dim, 2)
     errs = {}
-    precs = ("fp64", "mixed") if f != 0.0 else ("fp64", "mixed", "mixed_ff")
-    for prec in precs:
+    for prec in ("fp64", "mixed", "mixed_ff"):
         op = ew.WaveEquationOperation(m, k, precision=prec)
         errs[prec] = op.l2_error_post(torch.from_numpy(a.copy()).cuda(), amps, kv, t)
         op.close()
     assert ref > 0.0
     assert abs(errs["fp64"] - ref) <= 1e-8 * ref, (errs, ref)
     assert abs(errs["mixed"] - errs["fp64"]) <= 1e-4 * errs["fp64"], errs
-    if "mixed_ff" in errs:
-        assert abs(errs["mixed_ff"] - errs["fp64"]) <= 1e-8 * errs["fp64"], errs
+    assert abs(errs["mixed_ff"] - errs["fp64"]) <= 1e-8 * errs["fp64"], errs
 
 
 def test_post_error_rejects_null_state(env):
