@@ -1,7 +1,11 @@
 """Time loop of one solve on the GPU, mirroring WaveEquationProblem::run
 (explicit_wave.cc:549-813): mesh, time step, initial field, integrator,
-output of L2 errors at every tick."""
+output of L2 errors at every tick and, with ``write_vtu_output``, a VTU file
+of the solution and its error (output_results, explicit_wave.cc:336-406)."""
+import os
+
 from . import mesh as mesh_mod
+from . import vtu
 from .operator import WaveEquationOperation, reference_mode
 from .time_integrators import (SSPRK, AderAdconFull, ArbitraryHighOrderDG, ClassRK4, ExplicitEuler,
                                LowStorageRK33Reg2, LowStorageRK45Reg2, LowStorageRK45Reg3,
@@ -15,9 +19,14 @@ SUPPORTED = {"ExplEuler": ExplicitEuler, "clRK4": ClassRK4, "LSRK45R2": LowStora
              "ADERADCONFULL": AderAdconFull}
 
 
-def run(params, precision="fp64", on_output=None):
+# Name() of the reference's operators (wave_equation_operations.cc:105-167)
+OPERATOR_NAMES = {"ADER": "ADER", "ADERADCONFULL": "ADERADCONFULL"}
+
+
+def run(params, precision="fp64", on_output=None, output_dir="output"):
     """Run the parameter set; returns rows (time, step, err p, err u, |p|,
-    err p post) and the time step used.  ``params`` as returned by parameters.parse_prm."""
+    err p post) and the time step used.  ``params`` as returned by
+    parameters.parse_prm; VTU files go to ``output_dir``."""
     import torch
     integ = params["time_integrator"]
     if integ not in SUPPORTED:
@@ -44,6 +53,12 @@ def run(params, precision="fp64", on_output=None):
         e = op.l2_errors(sol, amps, kv, tc.time)
         post = op.l2_error_post(sol, amps, kv, tc.time)
         rows.append((tc.time, tc.time_step_number, e[0], e[1], e[2], post))
+        if params.get("write_vtu_output"):
+            name = vtu.output_name(k, OPERATOR_NAMES.get(integ, "Runge-Kutta"),
+                                   params.get("initital_cases", 1), params["n_refinements"],
+                                   int(tc.time / tc.tick_size))
+            vtu.write_vtu(os.path.join(output_dir, name), m, k, sol,
+                          exact=op.project_membrane(amps, kv, tc.time))
         if on_output:
             on_output(rows[-1])
 
