@@ -482,11 +482,17 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
   // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
   InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
   const int nstride = blockDim.x;
-  // Neighbour lines (u_e and p, both sides) of item wi that are not in the
-  // item's own block: asynchronous copies from L2 into this thread's slot.
-  auto prefetch_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
+  // With bulk copies usable and each field array of a cell a multiple of 16
+  // bytes (an even number of points per line), the same area holds whole
+  // neighbour field arrays instead: [(cell * 2 DIM + face) * 2 + (u_e, p)][N],
+  // filled by one bulk copy each, issued by warp 0 and completed on bars[3].
+  constexpr bool NB_BULK_OK = (N * sizeof(InT)) % 16 == 0;
+  const bool nb_bulk = NB_BULK_OK && ca.tma != 0;
+  InT* sNb = reinterpret_cast<InT*>(smem_cart + lay.nb);
+  const unsigned w0mask = blockDim.x >= 32 ? 0xffffffffu : ((1u << blockDim.x) - 1u);
+  // the neighbours of this thread's line (both sides); boundary: -id
+  auto lookup_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
     nbs[0] = nbs[1] = -EW_BC_HARD_WALL_ID;
-    const InT* Xg = static_cast<const InT*>(sd.X);
     if (tcl < wi.n_cells) {
       const int cell = wi.cell_begin + tcl;
 #pragma unroll
@@ -497,15 +503,55 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
           nb = cell;
         }
         nbs[s] = nb;
-        const int nl = nb - wi.cell_begin;
-        if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
-          const size_t o = (size_t)nb * F * N;
+      }
+    }
+  };
+  // warp 0: the item's neighbour arrays outside the block, one (cell, face)
+  // pair per lane; lane 0 announces the bytes first
+  auto issue_nb = [&](const WorkItem& wi, const SolveDesc& sd) {
+    const int lane = threadIdx.x;
+    const int pairs = wi.n_cells * 2 * DIM;
+    const InT* Xg = static_cast<const InT*>(sd.X);
+    constexpr uint32_t fbytes = (uint32_t)(N * sizeof(InT));
+    auto remote = [&](int q, int& nb) {
+      nb = sd.nbr[(size_t)(wi.cell_begin + q / (2 * DIM)) * 2 * DIM + q % (2 * DIM)];
+      const int nl = nb - wi.cell_begin;
+      return nb >= 0 && nb < sd.n_cells && !(nl >= 0 && nl < wi.n_cells);
+    };
+    uint32_t bytes = 0;
+    for (int q = lane; q < pairs; q += 32) {
+      int nb;
+      if (remote(q, nb)) bytes += 2 * fbytes;
+    }
+    bytes = __reduce_add_sync(w0mask, bytes);
+    if (lane == 0) mbar_expect_tx(&bars[3], bytes);
+    __syncwarp(w0mask);
+    for (int q = lane; q < pairs; q += 32) {
+      int nb;
+      if (remote(q, nb)) {
+        const int e = (q % (2 * DIM)) / 2;
+        const InT* src = Xg + (size_t)nb * F * N;
+        bulk_g2s(sNb + (size_t)(2 * q) * N, src + (size_t)e * N, fbytes, &bars[3]);
+        bulk_g2s(sNb + (size_t)(2 * q + 1) * N, src + (size_t)DIM * N, fbytes, &bars[3]);
+      }
+    }
+  };
+  // Neighbour lines (u_e and p, both sides) of item wi that are not in the
+  // item's own block: asynchronous copies from L2 into this thread's slot.
+  auto prefetch_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
+    lookup_nb(wi, sd, nbs);
+    const InT* Xg = static_cast<const InT*>(sd.X);
 #pragma unroll
-          for (int j = 0; j < NP; ++j) {
-            const size_t iu = o + te * N + tbase + j * tstr, ip = o + DIM * N + tbase + j * tstr;
-            cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, Xg + iu);
-            cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride, Xg + ip);
-          }
+    for (int s = 0; s < 2; ++s) {
+      const int nb = nbs[s];
+      const int nl = nb - wi.cell_begin;
+      if (tcl < wi.n_cells && nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
+        const size_t o = (size_t)nb * F * N;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          const size_t iu = o + te * N + tbase + j * tstr, ip = o + DIM * N + tbase + j * tstr;
+          cp_async<sizeof(InT)>(nslot + ((2 * s) * NP + j) * nstride, Xg + iu);
+          cp_async<sizeof(InT)>(nslot + ((2 * s + 1) * NP + j) * nstride, Xg + ip);
         }
       }
     }
@@ -516,6 +562,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     mbar_init(&bars[2], 1);
+    mbar_init(&bars[3], 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -525,6 +572,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
   uint32_t phase = 0;  // bit b: parity of the next wait on buffer b
   int it = 0;
   bool prev_a_ok = true;  // the previous item's accumulator copy arrived
+  bool prev_nb_ok = true;  // this thread saw the previous item's neighbour arrays arrive
+  int nb_last = -1;        // warp 0: item index of the last neighbour phase issued
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
     const int b = it & 1;
     const bool has_next = w + (int)gridDim.x < La.n_work;
@@ -570,23 +619,35 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     const bool tactive = tcl < nc;
     // this item's non-local neighbour lines: in flight during the bulk-copy
     // wait and the own-line contractions, awaited just before the fluxes
-    prefetch_nb(wi, sd, nbs);
+    if (nb_bulk) {
+      lookup_nb(wi, sd, nbs);
+      // a new phase only once every lane of warp 0 saw the previous one end
+      if (threadIdx.x < 32 && __all_sync(w0mask, prev_nb_ok)) {
+        issue_nb(wi, sd);
+        nb_last = it;
+      }
+    } else {
+      prefetch_nb(wi, sd, nbs);
+    }
     if (ca.tma) {
       const bool ok = mbar_wait(&bars[b], (phase >> b) & 1u);
       phase ^= (1u << b);
       // One barrier both ends the previous item (its pressure phase read the
       // accumulator buffer and, for float-pair input, the other X buffer)
       // and starts this one (cell constants written, X landed).
-      if (__syncthreads_or(!ok || !prev_a_ok)) {
+      if (__syncthreads_or(!ok || !prev_a_ok || !prev_nb_ok)) {
         // give up on this CTA's remaining items: wait (bounded) for the
         // copies still in flight, then leave
         if (threadIdx.x == 0) {
           atomicOr(La.err, ERR_WAIT_TIMEOUT);
           if (!ok) mbar_wait(&bars[b], ((phase >> b) & 1u) ^ 1u);
           if (a_single && it > 0) mbar_wait(&bars[2], (uint32_t)(it - 1) & 1u);
+          // neighbour arrays: the last phase issued (phases end in order)
+          if (nb_bulk && nb_last >= 0) mbar_wait(&bars[3], (uint32_t)nb_last & 1u);
         }
         cp_async_wait_all();
         prev_a_ok = true;
+        prev_nb_ok = true;
         break;
       }
       if (threadIdx.x == 0) {
@@ -699,7 +760,15 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
         ap = end_sum(ap);
         const Real tu[2] = {su + au, su - au};
         const Real tp[2] = {sp + ap, sp - ap};
-        cp_async_wait_all();  // this thread's neighbour lines
+        if (nb_bulk) {
+          // the item's neighbour arrays (bulk copies on bars[3])
+          if (!mbar_wait(&bars[3], (uint32_t)it & 1u)) {
+            atomicOr(La.err, ERR_WAIT_TIMEOUT);
+            prev_nb_ok = false;
+          }
+        } else {
+          cp_async_wait_all();  // this thread's neighbour lines
+        }
         // fluxes at both ends (without the face JxW)
         Real Fu[2], Fp[2];
 #pragma unroll
@@ -711,7 +780,16 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
           if (nb >= 0) {
             const int nl = nb - wi.cell_begin;
             Real vu = Real(0), vp = Real(0);
-            if (!(nl >= 0 && nl < nc)) {
+            if (!(nl >= 0 && nl < nc) && nb_bulk) {
+              // neighbour's line from its field arrays copied for this face
+              const InT* na = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * N + base;
+#pragma unroll
+              for (int j = 0; j < NP; ++j) {
+                const Real l = B.L[1 - s][j];
+                vu = mac(vu, l, to_real<Real>(na[j * str]));
+                vp = mac(vp, l, to_real<Real>(na[N + j * str]));
+              }
+            } else if (!(nl >= 0 && nl < nc)) {
               // neighbour's line from this thread's prefetch slot
 #pragma unroll
               for (int j = 0; j < NP; ++j) {
@@ -834,10 +912,11 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     prev_a_ok = a_ok;
   }
   // the last item's copies: none may be in flight when the block ends
-  if (__syncthreads_or(!prev_a_ok)) {
+  if (__syncthreads_or(!prev_a_ok || !prev_nb_ok)) {
     if (threadIdx.x == 0) {
       atomicOr(La.err, ERR_WAIT_TIMEOUT);
-      mbar_wait(&bars[2], (uint32_t)(it - 1) & 1u);
+      if (a_single && it > 0) mbar_wait(&bars[2], (uint32_t)(it - 1) & 1u);
+      if (nb_bulk && nb_last >= 0) mbar_wait(&bars[3], (uint32_t)nb_last & 1u);
     }
   }
 }
