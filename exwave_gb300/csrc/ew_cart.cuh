@@ -243,10 +243,26 @@ constexpr int kCellConsts = 4 + 3 + 6 * 2;
 
 // Shared-memory layout of the Cartesian kernel (bytes); AB is the size of
 // one staged accumulator element (8: FP64 or float pair, 4: the lo part).
+// Neighbour field arrays by bulk copy (else per-thread line copies): 3-D
+// with 4 or at least 6 points per line.  Measured per LSRK45 step (mixed,
+// about 226 M DoFs): k = 3 / 5 / 6 / 7 gain 1 / 6 / 8 / 6 %; k = 4 loses 4 %
+// (more registers for the window offsets) and k = 2 loses 37 % (108-byte
+// arrays: the copies' fixed cost dominates).
+template <int DIM, int NP>
+__host__ __device__ constexpr bool cart_nb_bulk() {
+  return DIM == 3 && (NP == 4 || NP >= 6);
+}
+
 template <int DIM, int NP, typename Real, typename InT, int AB = 8>
 struct CartSmem {
   static constexpr int N = ipow_c(NP, DIM);
   static constexpr int F = DIM + 1;
+  // one field array of a neighbour copied in bulk: the array rounded out to
+  // 16-byte boundaries at both ends (exactly the array when its size and
+  // start are multiples of 16)
+  static constexpr int NB_SLOT = (N * sizeof(InT)) % 16 == 0
+                                     ? (int)(N * sizeof(InT))
+                                     : (int)(((N * sizeof(InT) + 15) & ~(size_t)15) + 16);
   size_t bar, X, A, Kp, cell, nb, end;
   int xbytes, abytes;  // per buffer
   // The stage input X is double buffered (the next item's copy is in
@@ -263,10 +279,14 @@ struct CartSmem {
     abytes = stage_a ? CB * F * N * AB : 0;
     Kp = A + (a_single(stage_x, stage_a) ? 1 : 2) * (size_t)((abytes + 127) & ~127);
     cell = Kp + (size_t)DIM * CB * N * sizeof(Real);
-    // per thread: the neighbours' lines of u_e and p on both sides
+    // per thread: the neighbours' lines of u_e and p on both sides; or, with
+    // bulk copies, per (cell, face) the neighbour's u_e and p arrays in
+    // slots of NB_SLOT bytes
     nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
     const int threads = CB * DIM * ipow_c(NP, DIM - 1);
-    end = nb + (size_t)threads * 4 * NP * sizeof(InT);
+    const size_t lines = (size_t)threads * 4 * NP * sizeof(InT);
+    const size_t slots = cart_nb_bulk<DIM, NP>() ? (size_t)CB * 2 * DIM * 2 * NB_SLOT : 0;
+    end = nb + (lines > slots ? lines : slots);
     end = (end + 127) & ~(size_t)127;
   }
 };
@@ -482,13 +502,19 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
   // slot element k of this thread at k * blockDim.x + threadIdx.x (conflict-free)
   InT* nslot = reinterpret_cast<InT*>(smem_cart + lay.nb) + threadIdx.x;
   const int nstride = blockDim.x;
-  // With bulk copies usable and each field array of a cell a multiple of 16
-  // bytes (an even number of points per line), the same area holds whole
-  // neighbour field arrays instead: [(cell * 2 DIM + face) * 2 + (u_e, p)][N],
-  // filled by one bulk copy each, issued by warp 0 and completed on bars[3].
-  constexpr bool NB_BULK_OK = (N * sizeof(InT)) % 16 == 0;
-  const bool nb_bulk = NB_BULK_OK && ca.tma != 0;
-  InT* sNb = reinterpret_cast<InT*>(smem_cart + lay.nb);
+  // With bulk copies usable, the same area holds whole neighbour field
+  // arrays instead: slot (cell * 2 DIM + face) * 2 + (u_e, p), each filled by
+  // one bulk copy of the array rounded out to 16-byte boundaries, issued by
+  // warp 0 and completed on bars[3].  Bulk copies are enabled only when a
+  // cell's data is a multiple of 16 bytes, so that the rounded windows stay
+  // inside the stage input array.
+  constexpr int NB_SLOT = CartSmem<DIM, NP, Real, InT, A_ELEM>::NB_SLOT;
+  const bool nb_bulk = cart_nb_bulk<DIM, NP>() && ca.tma != 0;
+  unsigned char* sNb = smem_cart + lay.nb;
+  // byte offset of a neighbour's field array within its 16-byte window
+  auto nb_rem = [](int nb, int f) -> int {
+    return (int)((((size_t)nb * F + f) * N * sizeof(InT)) & 15);
+  };
   const unsigned w0mask = blockDim.x >= 32 ? 0xffffffffu : ((1u << blockDim.x) - 1u);
   // the neighbours of this thread's line (both sides); boundary: -id
   auto lookup_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
@@ -511,8 +537,14 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
   auto issue_nb = [&](const WorkItem& wi, const SolveDesc& sd) {
     const int lane = threadIdx.x;
     const int pairs = wi.n_cells * 2 * DIM;
-    const InT* Xg = static_cast<const InT*>(sd.X);
-    constexpr uint32_t fbytes = (uint32_t)(N * sizeof(InT));
+    const unsigned char* Xg = static_cast<const unsigned char*>(sd.X);
+    constexpr size_t fbytes = (size_t)N * sizeof(InT);
+    // the 16-byte window around field f of cell nb: start and length
+    auto window = [&](int nb, int f, size_t& w0) -> uint32_t {
+      const size_t s0 = ((size_t)nb * F + f) * fbytes;
+      w0 = s0 & ~(size_t)15;
+      return (uint32_t)(((s0 + fbytes + 15) & ~(size_t)15) - w0);
+    };
     auto remote = [&](int q, int& nb) {
       nb = sd.nbr[(size_t)(wi.cell_begin + q / (2 * DIM)) * 2 * DIM + q % (2 * DIM)];
       const int nl = nb - wi.cell_begin;
@@ -521,7 +553,10 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     uint32_t bytes = 0;
     for (int q = lane; q < pairs; q += 32) {
       int nb;
-      if (remote(q, nb)) bytes += 2 * fbytes;
+      if (remote(q, nb)) {
+        size_t w0;
+        bytes += window(nb, (q % (2 * DIM)) / 2, w0) + window(nb, DIM, w0);
+      }
     }
     bytes = __reduce_add_sync(w0mask, bytes);
     if (lane == 0) mbar_expect_tx(&bars[3], bytes);
@@ -529,10 +564,11 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     for (int q = lane; q < pairs; q += 32) {
       int nb;
       if (remote(q, nb)) {
-        const int e = (q % (2 * DIM)) / 2;
-        const InT* src = Xg + (size_t)nb * F * N;
-        bulk_g2s(sNb + (size_t)(2 * q) * N, src + (size_t)e * N, fbytes, &bars[3]);
-        bulk_g2s(sNb + (size_t)(2 * q + 1) * N, src + (size_t)DIM * N, fbytes, &bars[3]);
+        size_t w0;
+        uint32_t len = window(nb, (q % (2 * DIM)) / 2, w0);
+        bulk_g2s(sNb + (size_t)(2 * q) * NB_SLOT, Xg + w0, len, &bars[3]);
+        len = window(nb, DIM, w0);
+        bulk_g2s(sNb + (size_t)(2 * q + 1) * NB_SLOT, Xg + w0, len, &bars[3]);
       }
     }
   };
@@ -782,12 +818,14 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
             Real vu = Real(0), vp = Real(0);
             if (!(nl >= 0 && nl < nc) && nb_bulk) {
               // neighbour's line from its field arrays copied for this face
-              const InT* na = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * N + base;
+              const unsigned char* slot = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * NB_SLOT;
+              const InT* nu = reinterpret_cast<const InT*>(slot + nb_rem(nb, e)) + base;
+              const InT* np_ = reinterpret_cast<const InT*>(slot + NB_SLOT + nb_rem(nb, DIM)) + base;
 #pragma unroll
               for (int j = 0; j < NP; ++j) {
                 const Real l = B.L[1 - s][j];
-                vu = mac(vu, l, to_real<Real>(na[j * str]));
-                vp = mac(vp, l, to_real<Real>(na[N + j * str]));
+                vu = mac(vu, l, to_real<Real>(nu[j * str]));
+                vp = mac(vp, l, to_real<Real>(np_[j * str]));
               }
             } else if (!(nl >= 0 && nl < nc)) {
               // neighbour's line from this thread's prefetch slot
