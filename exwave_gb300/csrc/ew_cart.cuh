@@ -244,13 +244,14 @@ constexpr int kCellConsts = 4 + 3 + 6 * 2;
 // Shared-memory layout of the Cartesian kernel (bytes); AB is the size of
 // one staged accumulator element (8: FP64 or float pair, 4: the lo part).
 // Neighbour field arrays by bulk copy (else per-thread line copies): 3-D
-// with 4 or at least 6 points per line.  Measured per LSRK45 step (mixed,
-// about 226 M DoFs): k = 3 / 5 / 6 / 7 gain 1 / 6 / 8 / 6 %; k = 4 loses 4 %
-// (more registers for the window offsets) and k = 2 loses 37 % (108-byte
-// arrays: the copies' fixed cost dominates).
-template <int DIM, int NP>
+// with at least 6 points per line, and with 4 for FP32 stage inputs.
+// Measured per LSRK45 step (about 226 M DoFs): mixed k = 3 / 5 / 6 / 7 gain
+// 1 / 6 / 8 / 6 %, k = 4 loses 4 % (more registers for the window offsets)
+// and k = 2 loses 37 % (108-byte arrays: the copies' fixed cost dominates);
+// the compensated k = 3 kernel (8-byte inputs) lost 16 %.
+template <int DIM, int NP, typename InT>
 __host__ __device__ constexpr bool cart_nb_bulk() {
-  return DIM == 3 && (NP == 4 || NP >= 6);
+  return DIM == 3 && (NP >= 6 || (NP == 4 && sizeof(InT) == 4));
 }
 
 template <int DIM, int NP, typename Real, typename InT, int AB = 8>
@@ -285,7 +286,7 @@ struct CartSmem {
     nb = (cell + (size_t)CB * kCellConsts * sizeof(Real) + 15) & ~(size_t)15;
     const int threads = CB * DIM * ipow_c(NP, DIM - 1);
     const size_t lines = (size_t)threads * 4 * NP * sizeof(InT);
-    const size_t slots = cart_nb_bulk<DIM, NP>() ? (size_t)CB * 2 * DIM * 2 * NB_SLOT : 0;
+    const size_t slots = cart_nb_bulk<DIM, NP, InT>() ? (size_t)CB * 2 * DIM * 2 * NB_SLOT : 0;
     end = nb + (lines > slots ? lines : slots);
     end = (end + 127) & ~(size_t)127;
   }
@@ -509,7 +510,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
   // cell's data is a multiple of 16 bytes, so that the rounded windows stay
   // inside the stage input array.
   constexpr int NB_SLOT = CartSmem<DIM, NP, Real, InT, A_ELEM>::NB_SLOT;
-  const bool nb_bulk = cart_nb_bulk<DIM, NP>() && ca.tma != 0;
+  const bool nb_bulk = cart_nb_bulk<DIM, NP, InT>() && ca.tma != 0;
   unsigned char* sNb = smem_cart + lay.nb;
   // byte offset of a neighbour's field array within its 16-byte window
   auto nb_rem = [](int nb, int f) -> int {
