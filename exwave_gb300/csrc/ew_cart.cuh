@@ -203,6 +203,15 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+// transaction bytes announced without an arrival, and an arrival alone
+__device__ __forceinline__ void mbar_add_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
@@ -534,7 +543,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
     }
   };
   // warp 0: the item's neighbour arrays outside the block, one (cell, face)
-  // pair per lane; lane 0 announces the bytes first
+  // pair per lane and round of 32; each round's bytes are announced before
+  // its copies, and one arrival after the last round ends the phase
   auto issue_nb = [&](const WorkItem& wi, const SolveDesc& sd) {
     const int lane = threadIdx.x;
     const int pairs = wi.n_cells * 2 * DIM;
@@ -546,32 +556,30 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
       w0 = s0 & ~(size_t)15;
       return (uint32_t)(((s0 + fbytes + 15) & ~(size_t)15) - w0);
     };
-    auto remote = [&](int q, int& nb) {
-      nb = sd.nbr[(size_t)(wi.cell_begin + q / (2 * DIM)) * 2 * DIM + q % (2 * DIM)];
-      const int nl = nb - wi.cell_begin;
-      return nb >= 0 && nb < sd.n_cells && !(nl >= 0 && nl < wi.n_cells);
-    };
-    uint32_t bytes = 0;
-    for (int q = lane; q < pairs; q += 32) {
-      int nb;
-      if (remote(q, nb)) {
-        size_t w0;
-        bytes += window(nb, (q % (2 * DIM)) / 2, w0) + window(nb, DIM, w0);
+    for (int q0 = 0; q0 < pairs; q0 += 32) {
+      const int q = q0 + lane;
+      int nb = -1;
+      if (q < pairs) {
+        nb = sd.nbr[(size_t)(wi.cell_begin + q / (2 * DIM)) * 2 * DIM + q % (2 * DIM)];
+        const int nl = nb - wi.cell_begin;
+        if (!(nb >= 0 && nb < sd.n_cells && !(nl >= 0 && nl < wi.n_cells))) nb = -1;
+      }
+      size_t wu = 0, wp = 0;
+      uint32_t lu = 0, lp = 0;
+      if (nb >= 0) {
+        lu = window(nb, (q % (2 * DIM)) / 2, wu);
+        lp = window(nb, DIM, wp);
+      }
+      const uint32_t bytes = __reduce_add_sync(w0mask, lu + lp);
+      if (lane == 0 && bytes > 0) mbar_add_tx(&bars[3], bytes);
+      __syncwarp(w0mask);
+      if (nb >= 0) {
+        bulk_g2s(sNb + (size_t)(2 * q) * NB_SLOT, Xg + wu, lu, &bars[3]);
+        bulk_g2s(sNb + (size_t)(2 * q + 1) * NB_SLOT, Xg + wp, lp, &bars[3]);
       }
     }
-    bytes = __reduce_add_sync(w0mask, bytes);
-    if (lane == 0) mbar_expect_tx(&bars[3], bytes);
     __syncwarp(w0mask);
-    for (int q = lane; q < pairs; q += 32) {
-      int nb;
-      if (remote(q, nb)) {
-        size_t w0;
-        uint32_t len = window(nb, (q % (2 * DIM)) / 2, w0);
-        bulk_g2s(sNb + (size_t)(2 * q) * NB_SLOT, Xg + w0, len, &bars[3]);
-        len = window(nb, DIM, w0);
-        bulk_g2s(sNb + (size_t)(2 * q + 1) * NB_SLOT, Xg + w0, len, &bars[3]);
-      }
-    }
+    if (lane == 0) mbar_arrive(&bars[3]);
   };
   // Neighbour lines (u_e and p, both sides) of item wi that are not in the
   // item's own block: asynchronous copies from L2 into this thread's slot.
