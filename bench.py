@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--degrees", default="3,7", help="batch: degree range (inclusive)")
     ap.add_argument("--sizes", default="8,32", help="batch: cells per direction range (inclusive)")
     ap.add_argument("--quick", action="store_true",
-                    help="ader3d: timing only, without the run to T=0.5 on both paths")
+                    help="ader3d: timing only, without the run to T=0.5 on the three paths")
     return ap.parse_args()
 
 
