@@ -8,4 +8,4 @@ from .time_integrators import (SSPRK, AderAdconFull, ArbitraryHighOrderDG, Class
                                ExplicitEuler, LowStorageRK33Reg2, LowStorageRK45Reg2,
                                LowStorageRK45Reg3, LowStorageRK59Reg2)
 from .utilities import TimeControl  # noqa: F401
-from . import vtu  # noqa: F401
+from . import basis, vtu  # noqa: F401

@@ -22,7 +22,7 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_apply", "ew_rk_update", "ew_lsrk45_step", "ew_apply_ader", "ew_ader_step",
            "ew_quadrature_points", "ew_project_membrane", "ew_project_gaussian",
            "ew_l2_errors_membrane", "ew_l2_difference", "ew_hypercube_n_cells",
-           "ew_hypercube_mesh", "ew_synchronize", "ew_kernel_launches",
+           "ew_hypercube_mesh", "ew_nodal_to_gauss", "ew_gauss_to_nodal", "ew_synchronize", "ew_kernel_launches",
            "ew_batch_create", "ew_batch_destroy", "ew_batch_last_error", "ew_batch_solve_bytes",
            "ew_batch_bytes_free", "ew_batch_add", "ew_batch_remove", "ew_batch_set_state",
            "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_receivers",
@@ -100,6 +100,8 @@ def load():
         "ew_l2_difference": (ctypes.c_int, [vp, dp, dp, dp]),
         "ew_hypercube_n_cells": (i64, [ctypes.POINTER(HypercubeDesc)]),
         "ew_hypercube_mesh": (ctypes.c_int, [ctypes.POINTER(HypercubeDesc), dp, i32p]),
+        "ew_nodal_to_gauss": (ctypes.c_int, [i32, i32, i64, i32, dp, dp, dp]),
+        "ew_gauss_to_nodal": (ctypes.c_int, [i32, i32, i64, i32, dp, dp, dp]),
         "ew_synchronize": (ctypes.c_int, [vp]),
         "ew_kernel_launches": (i64, [vp]),
         "ew_tune_set": (ctypes.c_int, [i32, i32, i32, i32]),

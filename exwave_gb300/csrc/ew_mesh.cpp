@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/exwave_gb300.h"
+#include "ew_basis.h"
 
 namespace {
 
@@ -34,9 +35,72 @@ void multilinear(int dim, const double* V, const double* xi, double* x) {
   }
 }
 
+// Per-cell tensor-product interpolation: dst[c][f] = (M x M (x M)) src[c][f]
+// with the 1-D matrix M (n x n, row q = output point), points lexicographic.
+void tensor_interp(int dim, int n, int64_t n_cells, int n_fields, const std::vector<double>& M,
+                   const double* src, double* dst) {
+  const int64_t N = ipow64(n, dim);
+  std::vector<double> a((size_t)N), b((size_t)N);
+  for (int64_t cf = 0; cf < n_cells * n_fields; ++cf) {
+    const double* in = src + cf * N;
+    for (int64_t i = 0; i < N; ++i) a[i] = in[i];
+    for (int e = 0; e < dim; ++e) {
+      const int64_t str = ipow64(n, e);
+      for (int64_t i = 0; i < N; ++i) {
+        const int64_t j = (i / str) % n;      // this point's index along e
+        const int64_t base = i - j * str;     // the line's first point
+        double v = 0.0;
+        for (int l = 0; l < n; ++l) v += M[(size_t)j * n + l] * a[base + l * str];
+        b[i] = v;
+      }
+      a.swap(b);
+    }
+    double* out = dst + cf * N;
+    for (int64_t i = 0; i < N; ++i) out[i] = a[i];
+  }
+}
+
+// 1-D interpolation matrix from values at `from` to values at `to`
+std::vector<double> interp_matrix(const std::vector<double>& from, const std::vector<double>& to) {
+  const int n = (int)from.size();
+  std::vector<double> M((size_t)n * n);
+  for (int q = 0; q < n; ++q)
+    for (int j = 0; j < n; ++j) M[(size_t)q * n + j] = ew::lagrange(from, j, to[q]);
+  return M;
+}
+
+int nodal_convert(int dim, int degree, int64_t n_cells, int n_fields, const double* nodes,
+                  const double* src, double* dst, bool to_gauss) {
+  if ((dim != 2 && dim != 3) || degree < 1 || degree > 15 || n_cells < 0 || n_fields < 1 || !nodes)
+    return EW_ERR_INVALID;
+  if (n_cells > 0 && (!src || !dst || src == dst)) return EW_ERR_INVALID;
+  const int n = degree + 1;
+  std::vector<double> y(nodes, nodes + n);
+  for (int i = 0; i < n; ++i) {
+    if (!std::isfinite(y[i])) return EW_ERR_INVALID;
+    for (int j = 0; j < i; ++j)
+      if (!(std::fabs(y[i] - y[j]) > 1e-12)) return EW_ERR_INVALID;  // distinct nodes
+  }
+  const std::vector<double> g = ew::gauss_rule(n).x;
+  tensor_interp(dim, n, n_cells, n_fields, to_gauss ? interp_matrix(y, g) : interp_matrix(g, y), src,
+                dst);
+  return EW_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int ew_nodal_to_gauss(int32_t dim, int32_t degree, int64_t n_cells, int32_t n_fields,
+                      const double* nodes, const double* src, double* dst) {
+  return nodal_convert(dim, degree, n_cells, n_fields, nodes, src, dst, true);
+}
+
+int ew_gauss_to_nodal(int32_t dim, int32_t degree, int64_t n_cells, int32_t n_fields,
+                      const double* nodes, const double* src, double* dst) {
+  return nodal_convert(dim, degree, n_cells, n_fields, nodes, src, dst, false);
+}
+
 
 int64_t ew_hypercube_n_cells(const ew_hypercube_desc* d) {
   if (!valid(d)) return -1;

@@ -256,6 +256,23 @@ int64_t ew_hypercube_n_cells(const ew_hypercube_desc* desc);
  * neighbors[n_cells][2*dim] in the ew_mesh_desc conventions. */
 int ew_hypercube_mesh(const ew_hypercube_desc* desc, double* vertices, int32_t* neighbors);
 
+/* Change of nodal basis per cell, on the host, for adapters whose vectors
+ * hold Q_k by its values at other 1-D support points.  The reference's
+ * FE_DGQ(k) (explicit_wave.cc:162) uses k+1 equidistant points on [0,1];
+ * FEEvaluation interpolates those coefficients to QGauss(k+1) before the
+ * operator (wave_equation_operations.cc:411-419).  This library stores the
+ * Gauss-point values directly.  src and dst: host arrays
+ * [n_cells][n_fields][(k+1)^dim], points lexicographic (x fastest); `nodes`
+ * holds the k+1 distinct 1-D support points.  Both directions are exact
+ * (the same Q_k polynomial).  The caller still maps its own DoF numbering
+ * to this per-cell order.
+ *  ew_nodal_to_gauss: values at `nodes` -> values at the Gauss points
+ *  ew_gauss_to_nodal: the inverse */
+int ew_nodal_to_gauss(int32_t dim, int32_t degree, int64_t n_cells, int32_t n_fields,
+                      const double* nodes, const double* src, double* dst);
+int ew_gauss_to_nodal(int32_t dim, int32_t degree, int64_t n_cells, int32_t n_fields,
+                      const double* nodes, const double* src, double* dst);
+
 /* ---------------------------------------------------------------- batches
  * Many independent solves (uneven degree, mesh size, material, source) in
  * one device-resident batch: each step advances every unfinished solve by
