@@ -1,0 +1,28 @@
+"""bench.py's reference arm on the CPU: one JSON line with the contract's
+keys, the oracle timed on the host cores on the same metric and workload
+as the GPU arm."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
+                        "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference"
+    assert j["metric"] == "DoF-updates/s" and j["unit"] == "DoF-updates/s"
+    assert j["higher_is_better"] is True and j["steps"] == 1 and j["warmup"] == 1
+    assert j["value"] > 0 and j["ms_per_step"] > 0
+    assert j["e2e"] == {"value": j["value"], "unit": j["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    cb = j["cpu_baseline"]
+    assert cb["value"] == j["value"] and cb["kind"] in ("port", "reference")
+    assert cb["cores"] >= 1 and cb["sample"]
+    assert "workload" in j["config"]
