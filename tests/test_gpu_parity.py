@@ -229,6 +229,10 @@ EDGE = [
     (3, 5, 3, 0.0, 2, 4),                  # 27 cells, items of 4: the last holds 3
     (2, 4, 5, 0.0, [1, 1, 3, 3], 3),      # 25 cells, items of 3: the last holds 1
     (3, 3, 3, 0.1, 2, 5),                  # curved, 27 cells, items of 5
+    # axis-aligned 3-D degrees whose neighbour arrays come by bulk copy
+    (3, 3, 4, 0.0, [1, 2, 3, 1, 2, 3], 5),  # 64 cells, items of 5: the last holds 4
+    (3, 6, 3, 0.0, [3, 1, 2, 2, 1, 3], 2),  # 27 cells, items of 2: the last holds 1
+    (3, 7, 2, 0.0, [2, 3, 1, 1, 3, 2], 1),  # 8 cells, one per item
 ]
 
 
