@@ -1,0 +1,102 @@
+"""The serving loop's host logic (exwave_gb300.serve.Server.run) on the CPU,
+with a fake batch in place of the device runtime: FIFO admission under an
+HBM budget (waiting while a solve does not fit), retirement at the end
+time, receiver samples read once each, latency statistics, and errors
+other than "over budget" propagated."""
+import numpy as np
+import pytest
+
+from exwave_gb300 import _lib, serve
+
+
+class FakeBatch:
+    """Host stand-in of batch.Batch: a solve costs its DoF count in bytes."""
+
+    def __init__(self, budget):
+        self.budget, self.used, self.peak = budget, 0, 0
+        self.solves, self.next_id, self.admit_order = {}, 0, []
+        self.fail_code = None
+
+    def add(self, solve):
+        if self.fail_code is not None:
+            raise _lib.EwError(self.fail_code, "injected")
+        cost = solve.mesh.n_cells * 4 * (solve.degree + 1) ** 3
+        if self.used + cost > self.budget:
+            raise _lib.EwError(-4, "over budget")
+        sid = self.next_id
+        self.next_id += 1
+        self.solves[sid] = [solve, 0, cost]
+        self.used += cost
+        self.peak = max(self.peak, self.used)
+        self.admit_order.append(sid)
+        return sid
+
+    def remove(self, sid):
+        self.used -= self.solves.pop(sid)[2]
+
+    def steps_left(self):
+        left = [s.n_steps - d for s, d, _ in self.solves.values() if s.n_steps > d]
+        return min(left) if left else 0
+
+    def step(self, n):
+        for v in self.solves.values():
+            v[1] = min(v[0].n_steps, v[1] + n)
+
+    def synchronize(self):
+        pass
+
+    def info(self, sid):
+        s, d, _ = self.solves[sid]
+        return d, s.n_steps
+
+    def receivers(self, sid, first, count):
+        s = self.solves[sid][0]
+        return np.arange(first, first + count, dtype=float)[:, None] * np.ones(len(s.receivers))
+
+
+def _server(budget, steps_per_tick=3):
+    srv = serve.Server.__new__(serve.Server)
+    srv.batch = FakeBatch(budget)
+    srv.steps_per_tick = steps_per_tick
+    return srv
+
+
+def test_fifo_admission_under_budget_and_statistics():
+    reqs = serve.draw_requests(12, rate=0.0, seed=3, cells=(2, 4), end_time=(0.02, 0.06))
+    largest = max(r.dofs() for r in reqs)
+    srv = _server(budget=2 * largest)
+    stats = srv.run(reqs)
+    fb = srv.batch
+    assert stats["completed"] == stats["offered"] == 12
+    assert stats["backlog_at_end"] == 0 and stats["active_at_end"] == 0
+    # admitted in arrival (request id) order, never above the budget
+    assert fb.next_id == 12 and fb.peak <= fb.budget
+    admitted = sorted(reqs, key=lambda r: r.admitted)
+    assert [r.rid for r in admitted] == sorted(r.rid for r in reqs)
+    for r in reqs:
+        # every step's receiver sample read exactly once, in order
+        tr = np.concatenate(r.trace)
+        assert tr.shape == (r.n_steps, len(r.receivers))
+        assert np.array_equal(tr[:, 0], np.arange(r.n_steps))
+        assert r.arrival <= r.admitted <= r.finished
+    lat = np.array([r.finished - r.arrival for r in reqs])
+    assert stats["latency_p50_s"] == pytest.approx(np.percentile(lat, 50))
+    assert stats["latency_p99_s"] == pytest.approx(np.percentile(lat, 99))
+    assert stats["peak_active"] >= 1 and stats["ticks"] >= 1
+
+
+def test_other_errors_propagate():
+    reqs = serve.draw_requests(2, rate=0.0, seed=4, cells=(2, 3), end_time=(0.02, 0.03))
+    srv = _server(budget=1 << 40)
+    srv.batch.fail_code = -1
+    with pytest.raises(_lib.EwError):
+        srv.run(reqs)
+
+
+def test_time_limit_reports_the_backlog():
+    # nothing fits: the queue waits until the time limit ends the run
+    reqs = serve.draw_requests(3, rate=0.0, seed=5, cells=(3, 3), end_time=(0.02, 0.02))
+    srv = _server(budget=1)
+    stats = srv.run(reqs, time_limit=0.05)
+    assert stats["completed"] == 0 and stats["backlog_at_end"] == 3
+    assert stats["latency_p50_s"] is None
