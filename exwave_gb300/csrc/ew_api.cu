@@ -1208,12 +1208,17 @@ int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const doubl
   return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "rk_update launch");
 }
 
-int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
-  int rc = check(ctx);
-  if (rc) return rc;
-  if (!vec_n || !vec_np || vec_n == vec_np)
-    return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step: vec_n and vec_np must be distinct");
+namespace {
+// The five fused stages of one LowStorageRK45Reg2 step
+// (time_integrators.cc:235-283) with the integrator's scratch given by the
+// caller: T, the FP64 third register (FP64 path), or X0 / X1, the two stage
+// inputs used ping-pong (mixed and compensated paths: FP32 values or float
+// pairs).  Shared by ew_lsrk45_step (scratch owned by the context) and
+// ew_lsrk45_step_static (scratch in the static device array).
+int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double* T, float* X0,
+                  float* X1) {
   using namespace ew;
+  int rc;
   const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
   const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
                         0.0};
@@ -1224,7 +1229,6 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
     // the old accumulator in place (cell-local).
     double* N = vec_n;
     double* P = vec_np;
-    double* T = ctx->d_tmp64;
     struct S {
       const double* X;
       const double* A;
@@ -1240,8 +1244,6 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
   }
   // mixed: accumulator in vec_np (in place; on Cartesian meshes a float-float
   // pair between the stages, FP64 at the end), FP32 stage inputs ping-pong
-  float* X0 = ctx->d_x32[0];
-  float* X1 = ctx->d_x32[1];
   rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0],
                     f2[0], 1.0f);
   if (rc) return rc;
@@ -1253,6 +1255,15 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
     if (rc) return rc;
   }
   return EW_OK;
+}
+}  // namespace
+
+int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!vec_n || !vec_np || vec_n == vec_np)
+    return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step: vec_n and vec_np must be distinct");
+  return lsrk45_stages(ctx, dt, vec_n, vec_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1]);
 }
 
 int ew_vec_update(ew_ctx* ctx, double alpha, double* y, double beta, const double* x, double gamma,
@@ -1496,44 +1507,11 @@ int ew_lsrk45_step_static(ew_ctx* ctx, double dt, double* vec_n, double* vec_np)
                     std::to_string((long long)EW_STATIC_SCRATCH_MAX_DOFS) + " DoFs)");
   float* scratch = nullptr;
   if ((rc = static_scratch(ctx, &scratch))) return rc;
-  using namespace ew;
-  const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
-  const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
-                        0.0};
-  if (!ctx->mixed) {
-    // FP64: the third register of the two-register scheme lives in the array
-    double* N = vec_n;
-    double* P = vec_np;
-    double* T = reinterpret_cast<double*>(scratch);
-    struct S {
-      const double* X;
-      const double* A;
-      double* Xo;
-      double* Ao;
-    } st[5] = {{N, N, T, P}, {T, P, P, N}, {P, N, N, T}, {N, T, T, P}, {T, P, nullptr, P}};
-    for (int s = 0; s < 5; ++s) {
-      rc = launch_stage(ctx, STAGE_F64, s < 4 ? CV_F64_MID : CV_F64_LAST, st[s].A, st[s].X,
-                        st[s].Xo, st[s].Ao, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
-      if (rc) return rc;
-    }
-    return EW_OK;
-  }
-  // mixed: the two FP32 stage inputs live in the array (second one at a
-  // 256-byte aligned offset)
+  // FP64: the third register of the two-register scheme lives in the array;
+  // mixed: the two FP32 stage inputs (the second at a 256-byte aligned offset)
   const size_t off = ((size_t)ctx->n_dofs + 63) & ~(size_t)63;
-  float* X0 = scratch;
-  float* X1 = scratch + off;
-  rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0],
-                    f2[0], 1.0f);
-  if (rc) return rc;
-  const float* xin[4] = {X0, X1, X0, X1};
-  float* xout[4] = {X1, X0, X1, nullptr};
-  for (int s = 1; s < 5; ++s) {
-    rc = launch_stage(ctx, STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1],
-                      xout[s - 1], vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
-    if (rc) return rc;
-  }
-  return EW_OK;
+  return lsrk45_stages(ctx, dt, vec_n, vec_np, reinterpret_cast<double*>(scratch), scratch,
+                       scratch + off);
 }
 
 int ew_apply_ader(ew_ctx* ctx, double dt, const double* src, double* dst) {

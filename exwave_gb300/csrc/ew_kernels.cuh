@@ -574,6 +574,28 @@ __device__ __forceinline__ void ck_deriv(const Real* D, const Real* x, const Rea
   out[DIM] = c_sq * rho * div;
 }
 
+// Accumulator of the Taylor sum: a float pair on the FP32 path, else the
+// compute type (FP64 or float-float).
+template <typename Real>
+using CkAcc = std::conditional_t<std::is_same<Real, float>::value, FF, Real>;
+template <typename Acc, typename T>
+__device__ __forceinline__ void ck_acc_add(Acc& a, T v) {
+  if constexpr (is_ff_v<Acc> && !is_ff_v<T>) {
+    float s, e;
+    two_sum(a.hi, v, s, e);
+    a = FF(s, __fadd_rn(a.lo, e));
+  } else {
+    a += v;
+  }
+}
+template <typename OutT, typename Acc>
+__device__ __forceinline__ OutT ck_acc_out(Acc a) {
+  if constexpr (is_ff_v<Acc> && !is_ff_v<OutT>)
+    return static_cast<OutT>(__fadd_rn(a.hi, a.lo));
+  else
+    return static_cast<OutT>(a);
+}
+
 // Shared state of one CK work item.
 template <typename Real>
 struct CkState {
@@ -594,8 +616,8 @@ struct CkState {
 // derivative j = s + 2 at level r = s/2 (M = NP - 2r points per direction),
 // added to the level's contribution; after odd steps the field set is
 // L2-projected onto the next lower level (degree - 2).
-template <int DIM, int NP, typename Real, bool CART, int S, int NSTEPS>
-__device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Real* c0) {
+template <int DIM, int NP, typename Real, bool CART, int S, int NSTEPS, typename Acc>
+__device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Acc* c0) {
   constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
   constexpr int R = S / 2;
   constexpr int M = NP - 2 * R;
@@ -615,7 +637,7 @@ __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Rea
     for (int fld = 0; fld < F; ++fld) {
       st.sS[st.cl * F * N + fld * NM + st.q] = sn[fld];
       if constexpr (R == 0)
-        c0[fld] += f * sn[fld];
+        ck_acc_add(c0[fld], f * sn[fld]);
       else
         st.sm[st.C[R] + st.cl * F * NM + fld * NM + st.q] += f * sn[fld];
     }
@@ -626,13 +648,13 @@ __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Rea
       const Level<Real> Ln = get_level(st.sB, NP, R + 1);
       tensor_ct<DIM, Real, M - 2, M>(Ln.P, st.sS, F * N, st.sS, F * N, st.sT1, st.sT2, F * N, st.nc, F);
     }
-    ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS>(st, fac, c0);
+    ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS, Acc>(st, fac, c0);
   }
 }
 
 // Bottom-up: contribution of level R interpolated to level R-1 and added.
-template <int DIM, int NP, typename Real, int R>
-__device__ __forceinline__ void ck_gather(CkState<Real>& st, Real* c0) {
+template <int DIM, int NP, typename Real, int R, typename Acc>
+__device__ __forceinline__ void ck_gather(CkState<Real>& st, Acc* c0) {
   if constexpr (R >= 1) {
     constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
     constexpr int M = NP - 2 * R, MP = M + 2;
@@ -644,7 +666,7 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Real* c0) {
     if constexpr (R - 1 == 0) {
       if (st.active) {
 #pragma unroll
-        for (int fld = 0; fld < F; ++fld) c0[fld] += up[st.cl * F * N + fld * NMP + st.q];
+        for (int fld = 0; fld < F; ++fld) ck_acc_add(c0[fld], up[st.cl * F * N + fld * NMP + st.q]);
       }
     } else {
       for (int idx = threadIdx.x; idx < st.nc * F * NMP; idx += blockDim.x) {
@@ -654,7 +676,7 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Real* c0) {
       }
     }
     __syncthreads();
-    ck_gather<DIM, NP, Real, R - 1>(st, c0);
+    ck_gather<DIM, NP, Real, R - 1, Acc>(st, c0);
   }
 }
 
@@ -760,13 +782,33 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
         for (int fld = 0; fld < F; ++fld) d1[fld] = -o[fld];
       }
     }
-    // Taylor terms 0 and 1; the recursion starts from S = -du/dt
+    // Taylor terms 0 and 1; the recursion starts from S = -du/dt.  The
+    // Taylor sum is accumulated in the compute type, except on the FP32
+    // path, where it is a float pair: term 0 is dt * u from the FP64 state
+    // (both split exactly into pairs), and every later term is added with an
+    // error-free two-sum, so that the sum carries about 44 bits like the
+    // FP64 state it is added to; it is rounded once, to the FP32 stage input
+    // T of the second step.
     Real* sS = sm + lay.Sv;
-    Real c0[F];
+    using Acc = CkAcc<Real>;
+    Acc c0[F];
     if (active) {
+      const size_t gq = ((size_t)wi.cell_begin + cl) * F * N + q;
 #pragma unroll
       for (int fld = 0; fld < F; ++fld) {
-        c0[fld] = dtr * sX[cl * F * N + fld * N + q] + half_dt2 * d1[fld];
+        if constexpr (is_ff_v<Acc> && !is_ff_v<Real>) {
+          float uh, ul;
+          if constexpr (is_f64_v<InT>) {
+            f64_split(load_nc(static_cast<const double*>(sd.X) + gq + fld * N), uh, ul);
+          } else {
+            uh = sX[cl * F * N + fld * N + q];
+            ul = 0.f;
+          }
+          c0[fld] = FF::from_double(La.ck_dt_d) * FF(uh, ul);
+          ck_acc_add(c0[fld], half_dt2 * d1[fld]);
+        } else {
+          c0[fld] = dtr * sX[cl * F * N + fld * N + q] + half_dt2 * d1[fld];
+        }
         sS[cl * F * N + fld * N + q] = -d1[fld];
       }
     }
@@ -786,13 +828,13 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     st.active = active;
     st.rho = rho;
     st.c_sq = c_sq;
-    ck_steps<DIM, NP, Real, CART, 0, NSTEPS>(st, fac, c0);
-    ck_gather<DIM, NP, Real, RLAST>(st, c0);
+    ck_steps<DIM, NP, Real, CART, 0, NSTEPS, Acc>(st, fac, c0);
+    ck_gather<DIM, NP, Real, RLAST, Acc>(st, c0);
     if (active) {
       OutT* T = static_cast<OutT*>(sd.Xout);
       const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + q;
 #pragma unroll
-      for (int fld = 0; fld < F; ++fld) T[g0 + fld * N] = static_cast<OutT>(c0[fld]);
+      for (int fld = 0; fld < F; ++fld) T[g0 + fld * N] = ck_acc_out<OutT>(c0[fld]);
     }
   }
 }

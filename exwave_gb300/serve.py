@@ -38,15 +38,20 @@ class Request:
     finished: float = None
     trace: list = field(default_factory=list)
     samples_read: int = 0
+    rejected: str = None
+    solve: object = None
 
     def make_solve(self):
-        m = mesh_mod.hypercube(3, self.cells, speed=self.speed, density=self.density)
-        h = 1.0 / self.cells
-        self.dt = 0.25 * h / (self.speed * self.degree ** 1.5)
-        self.n_steps = max(1, int(np.ceil(self.end_time / self.dt - 1e-12)))
-        return Solve(m, self.degree, self.dt, self.n_steps,
-                     source=(list(self.source_pos), self.f0, 1.0 / self.f0, 1.0),
-                     receivers=self.receivers)
+        """The request's Solve (mesh and tables), built once and kept."""
+        if self.solve is None:
+            m = mesh_mod.hypercube(3, self.cells, speed=self.speed, density=self.density)
+            h = 1.0 / self.cells
+            self.dt = 0.25 * h / (self.speed * self.degree ** 1.5)
+            self.n_steps = max(1, int(np.ceil(self.end_time / self.dt - 1e-12)))
+            self.solve = Solve(m, self.degree, self.dt, self.n_steps,
+                               source=(list(self.source_pos), self.f0, 1.0 / self.f0, 1.0),
+                               receivers=self.receivers)
+        return self.solve
 
     def dofs(self):
         return self.cells ** 3 * 4 * (self.degree + 1) ** 3
@@ -88,6 +93,7 @@ class Server:
         queue = deque()
         active = {}
         done = []
+        rejected = []
         t0 = time.perf_counter()
         dof_updates = 0
         ticks = 0
@@ -104,8 +110,14 @@ class Server:
                 try:
                     sid = b.add(solve)
                 except _lib.EwError as e:
-                    if e.code in (-4, -6):   # over the HBM budget / slot limit: wait
+                    if e.code in (-4, -6) and active:   # over the HBM budget / slot limit: wait
                         break
+                    if e.code in (-4, -6):
+                        # does not fit even with no solve resident: it never will
+                        r.rejected = str(e)
+                        r.solve = None
+                        rejected.append(queue.popleft())
+                        continue
                     raise
                 r.admitted = time.perf_counter() - t0
                 active[sid] = r
@@ -128,6 +140,7 @@ class Server:
                     r.samples_read = steps
                 if steps >= total:
                     r.finished = time.perf_counter() - t0
+                    r.solve = None  # the host copy of the mesh is no longer needed
                     b.remove(sid)
                     del active[sid]
                     done.append(r)
@@ -137,7 +150,8 @@ class Server:
         lat = np.array([r.finished - r.arrival for r in done]) if done else np.array([])
         wait = np.array([r.admitted - r.arrival for r in done]) if done else np.array([])
         return {
-            "completed": len(done), "offered": len(requests), "wall_s": wall,
+            "completed": len(done), "offered": len(requests), "rejected": len(rejected),
+            "wall_s": wall,
             "solves_per_s": len(done) / wall if wall > 0 else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,

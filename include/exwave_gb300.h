@@ -178,7 +178,10 @@ int ew_sample_receivers(ew_ctx* ctx, const double* state, double* out);
  * device and fails when the pool holds the memory).  This entry point keeps
  * its stage scratch in one static device array of EW_STATIC_SCRATCH_BYTES
  * (64 MiB) that every GPU loading the library holds until exit, and calls no
- * allocator.  Limit: n_dofs <= EW_STATIC_SCRATCH_MAX_DOFS, larger contexts
+ * allocator.  The context itself still allocates its own integrator scratch
+ * once, in ew_create, like every context; what this entry point adds is a
+ * step that calls no allocator and uses the static array in place of the
+ * context's buffers.  Limit: n_dofs <= EW_STATIC_SCRATCH_MAX_DOFS, larger contexts
  * get EW_ERR_TOO_LARGE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
  * first call before any stream capture.  All calls on a device share the

@@ -1068,6 +1068,25 @@ void ewo_project_modes(ewo_problem* p, int n_modes, const double* amp, const int
     }
 }
 
+// Gaussian pressure pulse p = amp exp(-|x - x0|^2 / (2 width^2)), u = 0,
+// sampled at the Gauss points (the L2 projection in the collocation basis,
+// project_initial_field, wave_equation_operations.cc:902-935).  The pulse
+// itself has no counterpart in the reference; it is the initial field of
+// the curved two-layer ADER configuration.
+void ewo_project_gaussian(ewo_problem* p, const double* x0, double width, double amp, double* u) {
+  Oracle* O = reinterpret_cast<Oracle*>(p);
+  std::vector<double> xyz((size_t)O->mesh.n_cells * O->N * O->dim);
+  ewo_quadrature_points(p, xyz.data());
+  for (int64_t c = 0; c < O->mesh.n_cells; ++c)
+    for (int q = 0; q < O->N; ++q) {
+      const double* x = &xyz[((size_t)c * O->N + q) * O->dim];
+      double r2 = 0.0;
+      for (int e = 0; e < O->dim; ++e) r2 += (x[e] - x0[e]) * (x[e] - x0[e]);
+      for (int f = 0; f < O->dim; ++f) u[(size_t)c * O->F * O->N + f * O->N + q] = 0.0;
+      u[(size_t)c * O->F * O->N + O->dim * O->N + q] = amp * std::exp(-r2 / (2.0 * width * width));
+    }
+}
+
 void ewo_apply(ewo_problem* p, const double* src, double* dst, double boundary_fac) {
   reinterpret_cast<Oracle*>(p)->apply(src, dst, boundary_fac);
 }

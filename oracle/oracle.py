@@ -64,6 +64,7 @@ def lib():
         L.ewo_quadrature_points.argtypes = [P, dp]
         L.ewo_project_reference.argtypes = [P, ctypes.c_int, ctypes.c_double, dp]
         L.ewo_project_modes.argtypes = [P, ctypes.c_int, dp, ip, ctypes.c_double, dp]
+        L.ewo_project_gaussian.argtypes = [P, dp, ctypes.c_double, ctypes.c_double, dp]
         L.ewo_apply.argtypes = [P, dp, dp, ctypes.c_double]
         L.ewo_rk_update.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                     dp, dp, dp]
@@ -160,6 +161,19 @@ class Problem:
         u = self.zeros()
         lib().ewo_project_modes(self.h, len(amps), _dp(amps),
                                 kv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), t, _dp(u))
+        return u
+
+    def quadrature_points(self):
+        """Physical coordinates of every Gauss point, (n_cells, N, dim)."""
+        xyz = np.zeros(self.n_dofs // (self.dim + 1) * self.dim)
+        lib().ewo_quadrature_points(self.h, _dp(xyz))
+        return xyz.reshape(-1, (self.degree + 1) ** self.dim, self.dim)
+
+    def project_gaussian(self, x0, width, amp=1.0):
+        c = np.zeros(3)
+        c[:len(x0)] = x0
+        u = self.zeros()
+        lib().ewo_project_gaussian(self.h, _dp(c), width, amp, _dp(u))
         return u
 
     def apply(self, src, boundary_fac=1.0):

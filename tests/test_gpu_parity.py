@@ -15,6 +15,8 @@ pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-12
 MIXED_TOL = 2e-5
 FF_TOL = 1e-11
+MIXED_ADER_TOL = 5e-5
+MIXED_ADER_STEP_TOL = 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -144,10 +146,14 @@ def test_lsrk45_steps_call(env, case, precision, n_steps):
 
 @pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 5, 9, 10, 13)], ids=ids)
 @pytest.mark.parametrize("post", [False, True])
-@pytest.mark.parametrize("precision", ["fp64", "mixed_ff"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_ff", "mixed"])
 def test_ader_step(env, case, post, precision):
     """apply_ader and two ADER steps (± post) against the oracle, on the FP64
-    (1e-12 relative) and the compensated float-float path (1e-11 relative)."""
+    (1e-12 relative), the compensated float-float (1e-11 relative) and the
+    mixed path (FP32 operator with a float-pair Taylor sum: 5e-5 relative for
+    apply_ader, whose stage input T is itself rounded to FP32 -- measured up
+    to 2.3e-5; 1e-6 relative for the FP64 state after two steps, which adds
+    dt times such an application -- measured up to 1.4e-7)."""
     ew, oracle, torch = env
     dim, k, n, ref, f, bids, het = case
     m = make_case(ew, dim, n, ref, f, bids, het, seed=11)
@@ -162,9 +168,10 @@ def test_ader_step(env, case, post, precision):
     dst = torch.zeros_like(src)
     op.apply_ader(src, dst, dt)
     op.synchronize()
-    tol = FP64_TOL if precision == "fp64" else FF_TOL
+    tol = {"fp64": FP64_TOL, "mixed_ff": FF_TOL, "mixed": MIXED_ADER_TOL}[precision]
     err = np.abs(dst.cpu().numpy() - ref_dst).max() / np.abs(ref_dst).max()
     assert err < tol, err
+    tol = {"fp64": FP64_TOL, "mixed_ff": FF_TOL, "mixed": MIXED_ADER_STEP_TOL}[precision]
     # two full steps
     a, b = u0.copy(), np.zeros_like(u0)
     vn = torch.from_numpy(u0.copy()).cuda()
@@ -175,8 +182,9 @@ def test_ader_step(env, case, post, precision):
         op.ader_step(dt, vn, vnp)
         vn, vnp = vnp, vn
     op.synchronize()
-    err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
-    assert err < tol, err
+    err2 = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
+    print("ader %s post=%d: apply_ader %.3e, two steps %.3e" % (precision, post, err, err2))
+    assert err2 < tol, err2
 
 
 def test_rk_update_matches_reference_updater(env):

@@ -94,9 +94,46 @@ def test_other_errors_propagate():
 
 
 def test_time_limit_reports_the_backlog():
-    # nothing fits: the queue waits until the time limit ends the run
+    # the first request occupies the arena for longer than the time limit;
+    # the others wait behind it until the limit ends the run
+    reqs = serve.draw_requests(3, rate=0.0, seed=5, cells=(3, 3), end_time=(0.02, 0.02))
+    for r in reqs[1:]:
+        r.cells = 2
+    srv = _server(budget=reqs[0].dofs())
+    fb = srv.batch
+    fb.step = lambda n: None  # no progress: the first solve never ends
+    stats = srv.run(reqs, time_limit=0.05)
+    assert stats["completed"] == 0 and stats["backlog_at_end"] == 2
+    assert stats["active_at_end"] == 1 and stats["rejected"] == 0
+    assert stats["latency_p50_s"] is None
+
+
+def test_request_larger_than_the_arena_is_rejected():
+    """A request that does not fit even into the empty arena is rejected
+    (counted, not retried forever) and the others are served; without a time
+    limit the run ends."""
+    import threading
+    reqs = serve.draw_requests(5, rate=0.0, seed=6, cells=(2, 3), end_time=(0.02, 0.05))
+    reqs[2].cells = 9
+    budget = max(r.dofs() for i, r in enumerate(reqs) if i != 2)
+    srv = _server(budget=budget)
+    result = {}
+    t = threading.Thread(target=lambda: result.update(srv.run(reqs)), daemon=True)
+    t.start()
+    t.join(timeout=30)
+    assert not t.is_alive(), "the serving loop did not end"
+    assert result["rejected"] == 1 and result["completed"] == 4
+    assert reqs[2].rejected and reqs[2].finished is None
+    assert all(r.finished is not None for i, r in enumerate(reqs) if i != 2)
+
+
+def test_nothing_fits_ends_without_time_limit():
+    import threading
     reqs = serve.draw_requests(3, rate=0.0, seed=5, cells=(3, 3), end_time=(0.02, 0.02))
     srv = _server(budget=1)
-    stats = srv.run(reqs, time_limit=0.05)
-    assert stats["completed"] == 0 and stats["backlog_at_end"] == 3
-    assert stats["latency_p50_s"] is None
+    result = {}
+    t = threading.Thread(target=lambda: result.update(srv.run(reqs)), daemon=True)
+    t.start()
+    t.join(timeout=30)
+    assert not t.is_alive(), "the serving loop did not end"
+    assert result["completed"] == 0 and result["rejected"] == 3

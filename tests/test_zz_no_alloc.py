@@ -6,9 +6,12 @@ run under a fixed device-memory budget, and latency-sensitive loops, where
 cudaMalloc would synchronise the device or fail.  ew_lsrk45_step_static
 keeps its stage scratch in a static device array instead of the context's
 buffers; this test calls it through the C ABI, twice in a row, and checks
-every result against the regular ew_lsrk45_step with the tolerance of the
-other GPU tests, for both precisions, and that contexts above the array's
-size limit are rejected.  Named to run last in the suite.
+every result against the regular ew_lsrk45_step, for both precisions, on an
+axis-aligned 3-D mesh (the line kernel), a curved 3-D mesh (the staged
+curved-cell kernel) and a curved 2-D mesh, and that contexts above the
+array's size limit are rejected.  Both steps run the same kernels in the same
+order on the same inputs, only the scratch lives elsewhere, so the results
+must be bitwise equal.  Named to run last in the suite.
 """
 import ctypes
 
@@ -17,8 +20,12 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-FP64_TOL = 1e-12
-MIXED_TOL = 1e-12  # same kernels and inputs: the results agree to round-off
+MESHES = {
+    # dim, intervals, transform factor, boundary ids, degree
+    "cart3d": (3, 5, 0.0, [1, 2, 3, 1, 2, 3], 3),
+    "curved3d": (3, 4, 0.1, [3, 1, 2, 2, 1, 3], 4),
+    "curved2d": (2, 6, 0.15, [1, 2, 3, 2], 5),
+}
 
 
 @pytest.fixture(scope="module")
@@ -32,18 +39,19 @@ def env():
     return ew, _lib, torch
 
 
+@pytest.mark.parametrize("mesh", sorted(MESHES))
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_static_step_matches_regular_step(env, precision):
+def test_static_step_matches_regular_step(env, precision, mesh):
     ew, _lib, torch = env
     L = _lib.load()
-    m = ew.hypercube(3, 5, 0, 0.0, boundary_ids=[1, 2, 3, 1, 2, 3])
-    k = 3
+    dim, n, f, bids, k = MESHES[mesh]
+    m = ew.hypercube(dim, n, 0, f, boundary_ids=bids)
     op = ew.WaveEquationOperation(m, k, precision=precision)
     dt = ew.time_step_size(m, 0.25 / k ** 1.5)
-    u0 = op.project_membrane([1.0, 0.5], [[1, 1, 1], [2, 1, 3]])
+    kv = [[1, 1, 1], [2, 1, 3]] if dim == 3 else [[1, 1], [2, 3]]
+    u0 = op.project_membrane([1.0, 0.5], kv)
     ref_n, ref_np = u0.clone(), torch.zeros_like(u0)
     st_n, st_np = u0.clone(), torch.zeros_like(u0)
-    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
     for call in range(2):
         op.lsrk45_step(dt, ref_n, ref_np)
         rc = L.ew_lsrk45_step_static(op.ctx, dt, ctypes.c_void_p(st_n.data_ptr()),
@@ -53,8 +61,7 @@ def test_static_step_matches_regular_step(env, precision):
         ref = ref_np.cpu().numpy()
         got = st_np.cpu().numpy()
         assert np.abs(ref).max() > 0
-        err = np.abs(got - ref).max() / np.abs(ref).max()
-        assert err <= tol, (precision, call, err)
+        assert np.array_equal(got, ref), (precision, mesh, call, np.abs(got - ref).max())
         ref_n, ref_np = ref_np, ref_n
         st_n, st_np = st_np, st_n
 
