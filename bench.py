@@ -596,11 +596,12 @@ def main():
         if e64 is None:
             return None, None
         e = runs[prec]["errs"]
-        return (e[0] / e64[0] if e64[0] > 0 else None, e[1] / e64[1] if e64[1] > 0 else None)
+        return (float(e[0] / e64[0]) if e64[0] > 0 else None,
+                float(e[1] / e64[1]) if e64[1] > 0 else None)
 
     def matched(prec):
         rp, ru = ratio(prec)
-        return rp is not None and ru is not None and rp <= 1.1 and ru <= 1.1
+        return bool(rp is not None and ru is not None and rp <= 1.1 and ru <= 1.1)
 
     if args.precision == "auto":
         ok = [p for p in order if matched(p)]

@@ -26,6 +26,8 @@
 // work in float-float, about 44 significant bits on the FP32 pipes.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <type_traits>
 
@@ -136,6 +138,19 @@ struct CartConst<FF> {
   static __device__ __forceinline__ const CartBasis<FF>& get() { return c_cart_ff; }
 };
 
+// Magnitudes of the 1-D coefficients (their float parts) for the compensated
+// kernel: every anchored line sum (ew_ff.cuh) takes its anchor from
+// sum_j |c_j| |x_j| of its own terms, computed with these.
+struct FfBounds {
+  float aDP[4][4], aDQ[4][4], aDmc[4], aDmr[4];
+  float aTP[4][4], aTQ[4][4], aTmc[4], aTmr[4];
+  float aWs[4], aWa[4], aWmid;
+  float aLs[4], aLa[4], aLmid, aL[2][8];
+};
+namespace {
+__constant__ FfBounds c_ff_bounds;
+}  // namespace
+
 // Host: even-odd constants from the 1D Gauss data of NP points.
 inline CartBasis<double> make_cart_basis(int NP, const double* w, const double* D,
                                          const double* L0, const double* L1) {
@@ -163,6 +178,35 @@ inline CartBasis<double> make_cart_basis(int NP, const double* w, const double* 
     c.L[1][j] = L1[j];
   }
   return c;
+}
+
+inline FfBounds make_ff_bounds(const CartBasis<double>& c) {
+  FfBounds f;
+  for (int i = 0; i < 4; ++i) {
+    for (int j = 0; j < 4; ++j) {
+      f.aDP[i][j] = std::fabs((float)c.D.P[i][j]);
+      f.aDQ[i][j] = std::fabs((float)c.D.Q[i][j]);
+      f.aTP[i][j] = std::fabs((float)c.Dt.P[i][j]);
+      f.aTQ[i][j] = std::fabs((float)c.Dt.Q[i][j]);
+    }
+    f.aDmc[i] = std::fabs((float)c.D.mid_col[i]);
+    f.aDmr[i] = std::fabs((float)c.D.mid_row[i]);
+    f.aTmc[i] = std::fabs((float)c.Dt.mid_col[i]);
+    f.aTmr[i] = std::fabs((float)c.Dt.mid_row[i]);
+    f.aWs[i] = std::fabs((float)c.Ws[i]);
+    f.aWa[i] = std::fabs((float)c.Wa[i]);
+  }
+  f.aWmid = std::fabs((float)c.Wmid);
+  for (int j = 0; j < 4; ++j) {
+    f.aLs[j] = std::fabs((float)c.Ls[j]);
+    f.aLa[j] = std::fabs((float)c.La[j]);
+  }
+  f.aLmid = std::fabs((float)c.Lmid);
+  for (int j = 0; j < 8; ++j) {
+    f.aL[0][j] = std::fabs((float)c.L[0][j]);
+    f.aL[1][j] = std::fabs((float)c.L[1][j]);
+  }
+  return f;
 }
 
 template <typename Real>
@@ -443,8 +487,11 @@ struct CartArgs {
   int32_t tma;      // bulk copies usable (alignment checked on the host)
 };
 
+#ifndef EW_FF_MAXNREG
+#define EW_FF_MAXNREG 128
+#endif
 template <int DIM, int NP, typename Real, typename InT, int EPI>
-__global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >= 7 || sizeof(InT) == 8) ? 80 : 72)))
+__global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG : ((NP >= 7 || sizeof(InT) == 8) ? 80 : 72)))
     stage_cart_kernel(const CartArgs ca) {
   // next stage input: FP64, float pairs (compensated) or FP32
   using OutT = std::conditional_t<is_f64_v<Real>, double, std::conditional_t<is_ff_v<Real>, FF, float>>;
@@ -771,132 +818,328 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? 128 : ((NP >=
       const int cl = tcl, e = te, base = tbase, str = tstr;
       if (tactive) {
         const Real* cst = sCell + cl * kCellConsts;
-        const Real rho_inv = cst[0], rc2 = cst[1], tau_p = cst[2], itau = cst[3], ih = cst[4 + e];
         const int xo = cl * F * N;
-        Real xu[NP], xp[NP];
-#pragma unroll
-        for (int j = 0; j < NP; ++j) {
-          xu[j] = xval(xo + e * N + base + j * str);
-          xp[j] = xval(xo + DIM * N + base + j * str);
-        }
-        Real eu[4], ou[4], ep[4], op[4];
-#pragma unroll
-        for (int j = 0; j < H; ++j) {
-          eu[j] = xu[j] + xu[NP - 1 - j];
-          ou[j] = xu[j] - xu[NP - 1 - j];
-          ep[j] = xp[j] + xp[NP - 1 - j];
-          op[j] = xp[j] - xp[NP - 1 - j];
-        }
-        const Real um = (NP % 2) ? xu[NP / 2] : Real(0);
-        const Real pm = (NP % 2) ? xp[NP / 2] : Real(0);
-        // own traces at x_e = 0 (side 0) and x_e = 1 (side 1)
-        Real su = (NP % 2) ? B.Lmid * um : Real(0), au = Real(0);
-        Real sp = (NP % 2) ? B.Lmid * pm : Real(0), ap = Real(0);
-#pragma unroll
-        for (int j = 0; j < H; ++j) {
-          su = mac(su, B.Ls[j], eu[j]);
-          au = mac(au, B.La[j], ou[j]);
-          sp = mac(sp, B.Ls[j], ep[j]);
-          ap = mac(ap, B.La[j], op[j]);
-        }
-        su = end_sum(su);
-        au = end_sum(au);
-        sp = end_sum(sp);
-        ap = end_sum(ap);
-        const Real tu[2] = {su + au, su - au};
-        const Real tp[2] = {sp + ap, sp - ap};
-        if (nb_bulk) {
-          // the item's neighbour arrays (bulk copies on bars[3])
-          if (!mbar_wait(&bars[3], (uint32_t)it & 1u)) {
-            atomicOr(La.err, ERR_WAIT_TIMEOUT);
-            prev_nb_ok = false;
-          }
-        } else {
-          cp_async_wait_all();  // this thread's neighbour lines
-        }
-        // fluxes at both ends (without the face JxW)
-        Real Fu[2], Fp[2];
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          const Real nrm = s ? Real(1) : Real(-1);
-          const Real un_p = nrm * tu[s];
-          const int nb = nbs[s];
-          Real lambda;
-          if (nb >= 0) {
-            const int nl = nb - wi.cell_begin;
-            Real vu = Real(0), vp = Real(0);
-            if (!(nl >= 0 && nl < nc) && nb_bulk) {
-              // neighbour's line from its field arrays copied for this face
-              const unsigned char* slot = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * NB_SLOT;
-              const InT* nu = reinterpret_cast<const InT*>(slot + nb_rem(nb, e)) + base;
-              const InT* np_ = reinterpret_cast<const InT*>(slot + NB_SLOT + nb_rem(nb, DIM)) + base;
-#pragma unroll
-              for (int j = 0; j < NP; ++j) {
-                const Real l = B.L[1 - s][j];
-                vu = mac(vu, l, to_real<Real>(nu[j * str]));
-                vp = mac(vp, l, to_real<Real>(np_[j * str]));
-              }
-            } else if (!(nl >= 0 && nl < nc)) {
-              // neighbour's line from this thread's prefetch slot
-#pragma unroll
-              for (int j = 0; j < NP; ++j) {
-                const Real l = B.L[1 - s][j];
-                vu = mac(vu, l, to_real<Real>(nslot[((2 * s) * NP + j) * nstride]));
-                vp = mac(vp, l, to_real<Real>(nslot[((2 * s + 1) * NP + j) * nstride]));
-              }
-            } else {
-              // neighbour in this block: its trace on the opposite face, l_j(1-s)
-              const int no = nl * F * N;
-#pragma unroll
-              for (int j = 0; j < NP; ++j) {
-                const Real l = B.L[1 - s][j];
-                vu = mac(vu, l, xval(no + e * N + base + j * str));
-                vp = mac(vp, l, xval(no + DIM * N + base + j * str));
-              }
-            }
-            vu = end_sum(vu);
-            vp = end_sum(vp);
-            const Real tau_m = cst[7 + 2 * (2 * e + s)];
-            const Real tau_inv = cst[8 + 2 * (2 * e + s)];
-            const Real un_m = -nrm * vu;
-            lambda = (un_p + un_m + tau_p * tp[s] + tau_m * vp) * tau_inv;
-          } else {
-            const int id = -nb;
-            if (id == EW_BC_SOFT_WALL_ID) {
-              lambda = un_p * itau + tp[s];
-            } else if (id == EW_BC_ABSORBING_ID) {
-              lambda = Real(0.5) * tp[s] + Real(0.5) * un_p * itau;
-            } else {
-              if (id != EW_BC_HARD_WALL_ID) atomicOr(La.err, ERR_BAD_BOUNDARY_ID);
-              lambda = Real(0);
-            }
-          }
-          Fu[s] = (tp[s] - lambda) * rho_inv * nrm;
-          Fp[s] = rc2 * (-un_p + tau_p * (lambda - tp[s]));
-        }
-        // derivative of p and weighted transpose derivative of u_e
-        Real a1[4 + 1], b1[4], a2[4 + 1], b2[4];
-        eo_apply<NP, Real>(B.D, ep, op, pm, a1, b1);
-        eo_apply<NP, Real>(B.Dt, eu, ou, um, a2, b2);
-        const Real Fsu = Fu[0] + Fu[1], Fdu = Fu[0] - Fu[1];
-        const Real Fsp = Fp[0] + Fp[1], Fdp = Fp[0] - Fp[1];
-        const Real fu = bf * ih, fpp = bf * ih;
         Real ku[NP], kp[NP];
+        if constexpr (is_ff_v<Real>) {
+          // Compensated arithmetic with anchored sums (ew_ff.cuh): every
+          // line sum -- traces, derivative contractions with the face lifts
+          // folded in -- is accumulated on an anchor derived from the
+          // largest |value| on its line; the flux algebra uses unnormalised
+          // pairs.  The fluxes are written through q = t_p - lambda:
+          //   lift of u_e: -nrm q,  lift of p: -n.u - tau q,
+          // so that k_u = (-bf/h rho^-1) (D p + W G_u) and
+          // k_p = (bf/h rho c^2) (D^T u + W G_p).
+          const FfBounds& FB = c_ff_bounds;
+          const Real rho_inv = cst[0], rc2 = cst[1], tau_p = cst[2], itau = cst[3], ih = cst[4 + e];
+          FF xu[NP], xp[NP];
 #pragma unroll
-        for (int i = 0; i < H; ++i) {
-          // u_e: -rho^{-1} (D p)_i + lift; p: rho c^2 (Dt u)_i + lift
-          const Real ua = -rho_inv * a1[i] + B.Wa[i] * Fdu;
-          const Real ub = -rho_inv * b1[i] + B.Ws[i] * Fsu;
-          ku[i] = fu * (ua + ub);
-          ku[NP - 1 - i] = fu * (ub - ua);
-          const Real pa = rc2 * a2[i] + B.Wa[i] * Fdp;
-          const Real pb = rc2 * b2[i] + B.Ws[i] * Fsp;
-          kp[i] = fpp * (pa + pb);
-          kp[NP - 1 - i] = fpp * (pb - pa);
-        }
-        if constexpr (NP % 2 == 1) {
-          ku[H] = fu * (-rho_inv * a1[H] + B.Wmid * Fsu);
-          kp[H] = fpp * (rc2 * a2[H] + B.Wmid * Fsp);
+          for (int j = 0; j < NP; ++j) {
+            xu[j] = xval(xo + e * N + base + j * str);
+            xp[j] = xval(xo + DIM * N + base + j * str);
+          }
+          FF eu[4], ou[4], ep[4], op[4];
+#pragma unroll
+          for (int j = 0; j < H; ++j) {
+            eu[j] = ffu_add(xu[j], xu[NP - 1 - j]);
+            ou[j] = ffu_sub(xu[j], xu[NP - 1 - j]);
+            ep[j] = ffu_add(xp[j], xp[NP - 1 - j]);
+            op[j] = ffu_sub(xp[j], xp[NP - 1 - j]);
+          }
+          const FF um = (NP % 2) ? xu[NP / 2] : FF(0.f), pm = (NP % 2) ? xp[NP / 2] : FF(0.f);
+          // own traces at x_e = 0 (s + a) and x_e = 1 (s - a)
+          FF tu[2], tp[2];
+          {
+            float bsu = 0.f, bau = 0.f, bsp = 0.f, bap = 0.f;
+            if constexpr (NP % 2 == 1) {
+              bsu = FB.aLmid * fabsf(um.hi);
+              bsp = FB.aLmid * fabsf(pm.hi);
+            }
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+              bsu = __fmaf_rn(FB.aLs[j], fabsf(eu[j].hi), bsu);
+              bau = __fmaf_rn(FB.aLa[j], fabsf(ou[j].hi), bau);
+              bsp = __fmaf_rn(FB.aLs[j], fabsf(ep[j].hi), bsp);
+              bap = __fmaf_rn(FB.aLa[j], fabsf(op[j].hi), bap);
+            }
+            const float Su = anchor_for(fmaxf(bsu, bau)), Sp = anchor_for(fmaxf(bsp, bap));
+            AAcc su = aa_init(Su), au = aa_init(Su), sp = aa_init(Sp), ap = aa_init(Sp);
+            if constexpr (NP % 2 == 1) {
+              aa_add(su, B.Lmid, um);
+              aa_add(sp, B.Lmid, pm);
+            }
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+              aa_add(su, B.Ls[j], eu[j]);
+              aa_add(au, B.La[j], ou[j]);
+              aa_add(sp, B.Ls[j], ep[j]);
+              aa_add(ap, B.La[j], op[j]);
+            }
+            aa_pm(au, su, Su, tu[0], tu[1]);
+            aa_pm(ap, sp, Sp, tp[0], tp[1]);
+          }
+          if (nb_bulk) {
+            if (!mbar_wait(&bars[3], (uint32_t)it & 1u)) {
+              atomicOr(La.err, ERR_WAIT_TIMEOUT);
+              prev_nb_ok = false;
+            }
+          } else {
+            cp_async_wait_all();
+          }
+          // lift inputs of both faces
+          FF Gu[2], Gp[2];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            const FF un_p = s ? tu[1] : FF(-tu[0].hi, -tu[0].lo);  // nrm . u on this side
+            const int nb = nbs[s];
+            FF q;  // t_p - lambda
+            if (nb >= 0) {
+              const int nl = nb - wi.cell_begin;
+              FF nu[NP], np_[NP];
+              if (!(nl >= 0 && nl < nc) && nb_bulk) {
+                const unsigned char* slot = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * NB_SLOT;
+                const InT* pu = reinterpret_cast<const InT*>(slot + nb_rem(nb, e)) + base;
+                const InT* pp = reinterpret_cast<const InT*>(slot + NB_SLOT + nb_rem(nb, DIM)) + base;
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  nu[j] = to_real<FF>(pu[j * str]);
+                  np_[j] = to_real<FF>(pp[j * str]);
+                }
+              } else if (!(nl >= 0 && nl < nc)) {
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  nu[j] = to_real<FF>(nslot[((2 * s) * NP + j) * nstride]);
+                  np_[j] = to_real<FF>(nslot[((2 * s + 1) * NP + j) * nstride]);
+                }
+              } else {
+                const int no = nl * F * N;
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  nu[j] = xval(no + e * N + base + j * str);
+                  np_[j] = xval(no + DIM * N + base + j * str);
+                }
+              }
+              float bnu = 0.f, bnp = 0.f;
+#pragma unroll
+              for (int j = 0; j < NP; ++j) {
+                bnu = __fmaf_rn(FB.aL[1 - s][j], fabsf(nu[j].hi), bnu);
+                bnp = __fmaf_rn(FB.aL[1 - s][j], fabsf(np_[j].hi), bnp);
+              }
+              const float Snu = anchor_for(bnu), Snp = anchor_for(bnp);
+              AAcc vu = aa_init(Snu), vp = aa_init(Snp);
+#pragma unroll
+              for (int j = 0; j < NP; ++j) {
+                aa_add(vu, B.L[1 - s][j], nu[j]);
+                aa_add(vp, B.L[1 - s][j], np_[j]);
+              }
+              const FF vU = aa_value(vu, Snu), vP = aa_value(vp, Snp);
+              const Real tau_m = cst[7 + 2 * (2 * e + s)];
+              const Real tau_inv = cst[8 + 2 * (2 * e + s)];
+              // un_m = -nrm vu; t_p - lambda = (tau_m (t_p - v_p) - (un_p + un_m)) / (tau_p + tau_m)
+              const FF un_m = s ? FF(-vU.hi, -vU.lo) : vU;
+              q = ffu_mul(ffu_sub(ffu_mul(tau_m, ffu_sub(tp[s], vP)), ffu_add(un_p, un_m)), tau_inv);
+            } else {
+              const int id = -nb;
+              if (id == EW_BC_SOFT_WALL_ID) {
+                // lambda = un_p / tau + t_p
+                const FF t = ffu_mul(un_p, itau);
+                q = FF(-t.hi, -t.lo);
+              } else if (id == EW_BC_ABSORBING_ID) {
+                // lambda = (t_p + un_p / tau) / 2
+                const FF t = ffu_sub(tp[s], ffu_mul(un_p, itau));
+                q = FF(0.5f * t.hi, 0.5f * t.lo);
+              } else {
+                if (id != EW_BC_HARD_WALL_ID) atomicOr(La.err, ERR_BAD_BOUNDARY_ID);
+                q = tp[s];  // lambda = 0
+              }
+            }
+            Gu[s] = s ? FF(-q.hi, -q.lo) : q;
+            const FF g = ffu_add(un_p, ffu_mul(tau_p, q));
+            Gp[s] = FF(-g.hi, -g.lo);
+          }
+          const FF Gsu = ffu_add(Gu[0], Gu[1]), Gdu = ffu_sub(Gu[0], Gu[1]);
+          const FF Gsp = ffu_add(Gp[0], Gp[1]), Gdp = ffu_sub(Gp[0], Gp[1]);
+          const FF fh = ffu_norm(ffu_mul(ih, bf));
+          const FF c1n = ffu_norm(ffu_mul(fh, rho_inv));
+          const FF c1 = FF(-c1n.hi, -c1n.lo);
+          const FF c2 = ffu_norm(ffu_mul(fh, rc2));
+          // u_e: D p with the lifts of G_u; p: D^T u_e with the lifts of G_p
+          // Each output pair (a_i, b_i) gets its own anchor from the row's
+          // sum of |coefficient| |value| (float parts), which keeps the
+          // anchor within a factor 4 of the row's largest partial sum.
+          auto contract = [&](const EoMat<FF>& M, const float (*aP)[4], const float (*aQ)[4],
+                              const float* amc, const float* amr, const FF* ev, const FF* ov, FF xm,
+                              FF Gs, FF Gd, FF c, FF* k) {
+            float ae[4], ao[4];
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+              ae[j] = fabsf(ev[j].hi);
+              ao[j] = fabsf(ov[j].hi);
+            }
+            const float ags = fabsf(Gs.hi), agd = fabsf(Gd.hi), axm = fabsf(xm.hi);
+#pragma unroll
+            for (int i = 0; i < H; ++i) {
+              float ba = FB.aWa[i] * agd, bb = FB.aWs[i] * ags;
+              if constexpr (NP % 2 == 1) ba = __fmaf_rn(amc[i], axm, ba);
+#pragma unroll
+              for (int j = 0; j < H; ++j) {
+                ba = __fmaf_rn(aP[i][j], ae[j], ba);
+                bb = __fmaf_rn(aQ[i][j], ao[j], bb);
+              }
+              const float S = anchor_for(fmaxf(ba, bb));
+              AAcc a = aa_init(S), b = aa_init(S);
+#pragma unroll
+              for (int j = 0; j < H; ++j) {
+                aa_add(a, M.P[i][j], ev[j]);
+                aa_add(b, M.Q[i][j], ov[j]);
+              }
+              if constexpr (NP % 2 == 1) aa_add(a, M.mid_col[i], xm);
+              aa_add(a, B.Wa[i], Gd);
+              aa_add(b, B.Ws[i], Gs);
+              FF yp, ym;
+              aa_pm(a, b, S, yp, ym);
+              k[i] = ffu_mul(c, yp);
+              k[NP - 1 - i] = ffu_mul(c, ym);
+            }
+            if constexpr (NP % 2 == 1) {
+              float bm = FB.aWmid * ags;
+#pragma unroll
+              for (int j = 0; j < H; ++j) bm = __fmaf_rn(amr[j], ao[j], bm);
+              const float S = anchor_for(bm);
+              AAcc m = aa_init(S);
+#pragma unroll
+              for (int j = 0; j < H; ++j) aa_add(m, M.mid_row[j], ov[j]);
+              aa_add(m, B.Wmid, Gs);
+              k[H] = ffu_mul(c, aa_value(m, S));
+            }
+          };
+          contract(B.D, FB.aDP, FB.aDQ, FB.aDmc, FB.aDmr, ep, op, pm, Gsu, Gdu, c1, ku);
+          contract(B.Dt, FB.aTP, FB.aTQ, FB.aTmc, FB.aTmr, eu, ou, um, Gsp, Gdp, c2, kp);
+        } else {
+          const Real rho_inv = cst[0], rc2 = cst[1], tau_p = cst[2], itau = cst[3], ih = cst[4 + e];
+          Real xu[NP], xp[NP];
+#pragma unroll
+          for (int j = 0; j < NP; ++j) {
+            xu[j] = xval(xo + e * N + base + j * str);
+            xp[j] = xval(xo + DIM * N + base + j * str);
+          }
+          Real eu[4], ou[4], ep[4], op[4];
+#pragma unroll
+          for (int j = 0; j < H; ++j) {
+            eu[j] = xu[j] + xu[NP - 1 - j];
+            ou[j] = xu[j] - xu[NP - 1 - j];
+            ep[j] = xp[j] + xp[NP - 1 - j];
+            op[j] = xp[j] - xp[NP - 1 - j];
+          }
+          const Real um = (NP % 2) ? xu[NP / 2] : Real(0);
+          const Real pm = (NP % 2) ? xp[NP / 2] : Real(0);
+          // own traces at x_e = 0 (side 0) and x_e = 1 (side 1)
+          Real su = (NP % 2) ? B.Lmid * um : Real(0), au = Real(0);
+          Real sp = (NP % 2) ? B.Lmid * pm : Real(0), ap = Real(0);
+#pragma unroll
+          for (int j = 0; j < H; ++j) {
+            su = mac(su, B.Ls[j], eu[j]);
+            au = mac(au, B.La[j], ou[j]);
+            sp = mac(sp, B.Ls[j], ep[j]);
+            ap = mac(ap, B.La[j], op[j]);
+          }
+          su = end_sum(su);
+          au = end_sum(au);
+          sp = end_sum(sp);
+          ap = end_sum(ap);
+          const Real tu[2] = {su + au, su - au};
+          const Real tp[2] = {sp + ap, sp - ap};
+          if (nb_bulk) {
+            // the item's neighbour arrays (bulk copies on bars[3])
+            if (!mbar_wait(&bars[3], (uint32_t)it & 1u)) {
+              atomicOr(La.err, ERR_WAIT_TIMEOUT);
+              prev_nb_ok = false;
+            }
+          } else {
+            cp_async_wait_all();  // this thread's neighbour lines
+          }
+          // fluxes at both ends (without the face JxW)
+          Real Fu[2], Fp[2];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            const Real nrm = s ? Real(1) : Real(-1);
+            const Real un_p = nrm * tu[s];
+            const int nb = nbs[s];
+            Real lambda;
+            if (nb >= 0) {
+              const int nl = nb - wi.cell_begin;
+              Real vu = Real(0), vp = Real(0);
+              if (!(nl >= 0 && nl < nc) && nb_bulk) {
+                // neighbour's line from its field arrays copied for this face
+                const unsigned char* slot = sNb + (size_t)(2 * (cl * 2 * DIM + 2 * e + s)) * NB_SLOT;
+                const InT* nu = reinterpret_cast<const InT*>(slot + nb_rem(nb, e)) + base;
+                const InT* np_ = reinterpret_cast<const InT*>(slot + NB_SLOT + nb_rem(nb, DIM)) + base;
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  const Real l = B.L[1 - s][j];
+                  vu = mac(vu, l, to_real<Real>(nu[j * str]));
+                  vp = mac(vp, l, to_real<Real>(np_[j * str]));
+                }
+              } else if (!(nl >= 0 && nl < nc)) {
+                // neighbour's line from this thread's prefetch slot
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  const Real l = B.L[1 - s][j];
+                  vu = mac(vu, l, to_real<Real>(nslot[((2 * s) * NP + j) * nstride]));
+                  vp = mac(vp, l, to_real<Real>(nslot[((2 * s + 1) * NP + j) * nstride]));
+                }
+              } else {
+                // neighbour in this block: its trace on the opposite face, l_j(1-s)
+                const int no = nl * F * N;
+#pragma unroll
+                for (int j = 0; j < NP; ++j) {
+                  const Real l = B.L[1 - s][j];
+                  vu = mac(vu, l, xval(no + e * N + base + j * str));
+                  vp = mac(vp, l, xval(no + DIM * N + base + j * str));
+                }
+              }
+              vu = end_sum(vu);
+              vp = end_sum(vp);
+              const Real tau_m = cst[7 + 2 * (2 * e + s)];
+              const Real tau_inv = cst[8 + 2 * (2 * e + s)];
+              const Real un_m = -nrm * vu;
+              lambda = (un_p + un_m + tau_p * tp[s] + tau_m * vp) * tau_inv;
+            } else {
+              const int id = -nb;
+              if (id == EW_BC_SOFT_WALL_ID) {
+                lambda = un_p * itau + tp[s];
+              } else if (id == EW_BC_ABSORBING_ID) {
+                lambda = Real(0.5) * tp[s] + Real(0.5) * un_p * itau;
+              } else {
+                if (id != EW_BC_HARD_WALL_ID) atomicOr(La.err, ERR_BAD_BOUNDARY_ID);
+                lambda = Real(0);
+              }
+            }
+            Fu[s] = (tp[s] - lambda) * rho_inv * nrm;
+            Fp[s] = rc2 * (-un_p + tau_p * (lambda - tp[s]));
+          }
+          // derivative of p and weighted transpose derivative of u_e
+          Real a1[4 + 1], b1[4], a2[4 + 1], b2[4];
+          eo_apply<NP, Real>(B.D, ep, op, pm, a1, b1);
+          eo_apply<NP, Real>(B.Dt, eu, ou, um, a2, b2);
+          const Real Fsu = Fu[0] + Fu[1], Fdu = Fu[0] - Fu[1];
+          const Real Fsp = Fp[0] + Fp[1], Fdp = Fp[0] - Fp[1];
+          const Real fu = bf * ih, fpp = bf * ih;
+#pragma unroll
+          for (int i = 0; i < H; ++i) {
+            // u_e: -rho^{-1} (D p)_i + lift; p: rho c^2 (Dt u)_i + lift
+            const Real ua = -rho_inv * a1[i] + B.Wa[i] * Fdu;
+            const Real ub = -rho_inv * b1[i] + B.Ws[i] * Fsu;
+            ku[i] = fu * (ua + ub);
+            ku[NP - 1 - i] = fu * (ub - ua);
+            const Real pa = rc2 * a2[i] + B.Wa[i] * Fdp;
+            const Real pb = rc2 * b2[i] + B.Ws[i] * Fsp;
+            kp[i] = fpp * (pa + pb);
+            kp[NP - 1 - i] = fpp * (pb - pa);
+          }
+          if constexpr (NP % 2 == 1) {
+            ku[H] = fu * (-rho_inv * a1[H] + B.Wmid * Fsu);
+            kp[H] = fpp * (rc2 * a2[H] + B.Wmid * Fsp);
+          }
         }
         // pressure part of this direction to shared memory
 #pragma unroll

@@ -142,6 +142,71 @@ __device__ __forceinline__ FF ff_norm(FF v) {
   return r;
 }
 
+// ---- unnormalised pair arithmetic -------------------------------------------
+// Sums and products whose lo part is left as computed (no renormalisation).
+// Every error stays below about 2^-48 times the operands' magnitude, which is
+// what the operator needs: its accuracy is measured against the size of the
+// values on a line, not against each intermediate result.
+__device__ __forceinline__ FF ffu_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return FF(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF ffu_sub(FF a, FF b) { return ffu_add(a, FF(-b.hi, -b.lo)); }
+__device__ __forceinline__ FF ffu_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return FF(p, e);
+}
+__device__ __forceinline__ FF ffu_norm(FF v) {
+  FF r;
+  fast_two_sum(v.hi, v.lo, r.hi, r.lo);
+  return r;
+}
+
+// ---- anchored sums of products ----------------------------------------------
+// A dot product sum_j c_j x_j of float pairs, accumulated on top of an anchor
+// S, a power of two with S >= 2 sum_j |c_j x_j| (so every partial sum plus S
+// stays in [S/2, 3S/2]).  With acc' = fma(c, x, acc) the increment actually
+// taken, t = acc' - acc, is exact (both lie on the grid of S 2^-24 and differ
+// by less than S), and r = fma(c, x, -t) is the part of the exact product
+// c x that acc' missed, |r| <= S 2^-24, rounded once.  r and the cross terms
+// of the pairs' lo parts go to a plain float sum lo.  The result
+// (acc - S) + lo, an unevaluated pair, carries an error of about
+// n^2 2^-48 S: the same size as a float-float dot product's, at half of its
+// instructions (6 per term against the two-sum's 12).  Two sums on the same
+// anchor also add exactly: (acc_a - S) + (acc_b - S) is a float.
+struct AAcc {
+  float a, l;
+};
+__device__ __forceinline__ AAcc aa_init(float S) { return AAcc{S, 0.f}; }
+__device__ __forceinline__ void aa_add(AAcc& s, FF c, FF x) {
+  const float a1 = __fmaf_rn(c.hi, x.hi, s.a);
+  const float t = __fsub_rn(a1, s.a);
+  const float r = __fmaf_rn(c.hi, x.hi, -t);
+  float l = __fadd_rn(s.l, r);
+  l = __fmaf_rn(c.lo, x.hi, l);
+  l = __fmaf_rn(c.hi, x.lo, l);
+  s.a = a1;
+  s.l = l;
+}
+// the sum as a pair (acc - S is exact)
+__device__ __forceinline__ FF aa_value(const AAcc& s, float S) { return FF(__fsub_rn(s.a, S), s.l); }
+// y_i = a_i + b_i and y_{n-1-i} = b_i - a_i of two sums on the same anchor:
+// exact in the hi parts
+__device__ __forceinline__ void aa_pm(const AAcc& a, const AAcc& b, float S, FF& plus, FF& minus) {
+  const float ha = __fsub_rn(a.a, S), hb = __fsub_rn(b.a, S);
+  plus = FF(__fadd_rn(hb, ha), __fadd_rn(b.l, a.l));
+  minus = FF(__fsub_rn(hb, ha), __fsub_rn(b.l, a.l));
+}
+// the smallest power of two >= 2 (1 + 2^-20) bound, for bound >= 0 (0 for 0)
+__device__ __forceinline__ float anchor_for(float bound) {
+  const float b = __fmul_rn(bound, 2.000002f);
+  return __uint_as_float((__float_as_uint(b) + 0x007fffffu) & 0xff800000u);
+}
+
 // read-only load of a pair (8-byte aligned: arrays of FF)
 template <>
 __device__ __forceinline__ FF load_nc<FF>(const FF* p) {

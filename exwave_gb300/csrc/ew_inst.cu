@@ -137,7 +137,10 @@ cudaError_t set_constants(const double* w, const double* D, const double* L0, co
   e = cudaMemcpyToSymbol(c_cart_f, &cf, sizeof(cf));
   if (e != cudaSuccess) return e;
   const CartBasis<FF> cff = cast_basis<FF>(cd);
-  return cudaMemcpyToSymbol(c_cart_ff, &cff, sizeof(cff));
+  e = cudaMemcpyToSymbol(c_cart_ff, &cff, sizeof(cff));
+  if (e != cudaSuccess) return e;
+  const FfBounds fb = make_ff_bounds(cd);
+  return cudaMemcpyToSymbol(c_ff_bounds, &fb, sizeof(fb));
 }
 
 template <class K>
