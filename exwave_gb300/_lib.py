@@ -15,7 +15,7 @@ STATUS = {0: "EW_OK", -1: "EW_ERR_INVALID", -2: "EW_ERR_UNSUPPORTED", -3: "EW_ER
 EW_PREC_FP64 = 0
 EW_PREC_MIXED = 1
 EW_PREC_MIXED_FF = 2
-EW_MAX_DEGREE = 7
+EW_MAX_DEGREE = 12
 
 # every entry point declared in include/exwave_gb300.h
 EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_dofs", "ew_n_cells",

@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-PAIRS = [(d, n) for d in (2, 3) for n in range(2, 9)]
+PAIRS = [(d, n) for d in (2, 3) for n in range(2, 14)]
 
 
 def nvcc():

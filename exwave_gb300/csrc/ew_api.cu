@@ -22,25 +22,17 @@
 namespace ew {
 
 namespace {
-KernelTable g_tables[2][9];
+KernelTable g_tables[2][EW_MAX_DEGREE + 2];
 std::once_flag g_tables_once;
 
+#define EW_REG(d, n) kernel_table_d##d##_##n(g_tables[d - 2][n]);
 void init_tables() {
-  kernel_table_d2_2(g_tables[0][2]);
-  kernel_table_d2_3(g_tables[0][3]);
-  kernel_table_d2_4(g_tables[0][4]);
-  kernel_table_d2_5(g_tables[0][5]);
-  kernel_table_d2_6(g_tables[0][6]);
-  kernel_table_d2_7(g_tables[0][7]);
-  kernel_table_d2_8(g_tables[0][8]);
-  kernel_table_d3_2(g_tables[1][2]);
-  kernel_table_d3_3(g_tables[1][3]);
-  kernel_table_d3_4(g_tables[1][4]);
-  kernel_table_d3_5(g_tables[1][5]);
-  kernel_table_d3_6(g_tables[1][6]);
-  kernel_table_d3_7(g_tables[1][7]);
-  kernel_table_d3_8(g_tables[1][8]);
+  EW_REG(2, 2) EW_REG(2, 3) EW_REG(2, 4) EW_REG(2, 5) EW_REG(2, 6) EW_REG(2, 7) EW_REG(2, 8)
+  EW_REG(2, 9) EW_REG(2, 10) EW_REG(2, 11) EW_REG(2, 12) EW_REG(2, 13)
+  EW_REG(3, 2) EW_REG(3, 3) EW_REG(3, 4) EW_REG(3, 5) EW_REG(3, 6) EW_REG(3, 7) EW_REG(3, 8)
+  EW_REG(3, 9) EW_REG(3, 10) EW_REG(3, 11) EW_REG(3, 12) EW_REG(3, 13)
 }
+#undef EW_REG
 }  // namespace
 
 const KernelTable& kernel_table(int dim, int np) {
@@ -554,6 +546,9 @@ struct ew_ctx {
   int64_t n_cells = 0, n_dofs = 0;
   bool mixed = false, cart = false, post = false;
   bool ff = false;  // compensated operator (float-float arithmetic, FP32 data)
+  // axis-aligned cells served by the line kernel (it is built for every
+  // degree in 2-D and up to degree 7 in 3-D; otherwise the generic kernel)
+  bool line = false;
   int cb_stage = 1, cb_ck = 1;
   const ew::KernelTable* kt = nullptr;
   int32_t* d_nbr = nullptr;
@@ -642,9 +637,7 @@ int validate_mesh_impl(const ew_mesh_desc* m, bool* cartesian) {
   if (!m) return fail(nullptr, EW_ERR_INVALID, "mesh is NULL");
   if (m->dim != 2 && m->dim != 3) return fail(nullptr, EW_ERR_INVALID, "dim must be 2 or 3");
   if (m->degree < 1 || m->degree > EW_MAX_DEGREE)
-    return fail(nullptr, m->degree > EW_MAX_DEGREE && m->degree <= 12 ? EW_ERR_UNSUPPORTED
-                                                                      : EW_ERR_INVALID,
-                "degree must be in 1.." + std::to_string(EW_MAX_DEGREE));
+    return fail(nullptr, EW_ERR_INVALID, "degree must be in 1.." + std::to_string(EW_MAX_DEGREE));
   if (m->n_cells < 1 || m->n_cells > (int64_t)0x7fffffff)
     return fail(nullptr, EW_ERR_INVALID, "n_cells out of range");
   if (!m->vertices || !m->neighbors || !m->speed || !m->density)
@@ -768,7 +761,8 @@ bool cart_variant_in32(int cv) {
          cv == ew::CV_MIX_UPD || cv == ew::CV_MIX_LAST_FF || cv == ew::CV_MIX_S1_FF;
 }
 bool cart_variant_apply(int cv) {
-  return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32;
+  return cv == ew::CV_F64_APPLY || cv == ew::CV_MIX_APPLY64 || cv == ew::CV_MIX_APPLY32 ||
+         cv == ew::CV_FF_APPLY64 || cv == ew::CV_FF_APPLYFF;
 }
 
 // One operator launch.  `variant` selects the general (curved-cell) kernel,
@@ -798,12 +792,13 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
       case ew::CV_MIX_LAST: cvar = ew::CV_FF_LAST; break;
       case ew::CV_MIX_UPD: cvar = ew::CV_FF_UPD; break;
       case ew::CV_MIX_APPLY32: cvar = ew::CV_FF_APPLYFF; break;
+      case ew::CV_FF_LAST_PAIR: break;
       default:
         return fail(c, EW_ERR_UNSUPPORTED, "this operation is not built for EW_PREC_MIXED_FF");
     }
     variant = variant == ew::STAGE_MIX_IN64 ? ew::STAGE_FF_IN64 : ew::STAGE_FF_INFF;
   }
-  if (c->cart) {
+  if (c->line) {
     // line kernel: stage X unless it is the accumulator itself (first LSRK
     // stage); bulk copies need 16-byte alignment
     const size_t in_sz = cart_variant_in32(cvar) ? 4 : 8;
@@ -822,7 +817,8 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
     const int grid = std::max(1, std::min(c->n_work_cart, occ * c->num_sms));
     e = k.launch(a, sx, tma ? 1 : 0, grid, c->stream);
   } else {
-    const ew::KernelEntry& k = c->kt->stage[variant][0];
+    const ew::KernelEntry& k = c->kt->stage[variant][c->cart ? 1 : 0];
+    if (!k.launch) return fail(c, EW_ERR_UNSUPPORTED, "no stage kernel built for this mesh and precision");
     e = k.launch(a, c->grid_stage[variant], c->stream);
   }
   ++c->launches;
@@ -843,13 +839,16 @@ int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
   a.ck_dt = (float)dt;
   a.ck_half_dt2 = (float)(0.5 * dt * dt);
   double fac = -0.5, dtp = dt * dt * dt;
-  for (int s = 0; s < 8; ++s) {
+  for (int s = 0; s < 12; ++s) {
     fac /= -(s + 3.0);
     a.ck_fac_d[s] = fac * dtp;
     a.ck_fac[s] = (float)(fac * dtp);
     dtp *= dt;
   }
   const ew::KernelEntry& k = c->kt->ck[c->ff ? 2 : (c->mixed ? 1 : 0)][c->cart ? 1 : 0][c->post ? 1 : 0];
+  if (!k.launch)
+    return fail(c, EW_ERR_UNSUPPORTED,
+                "ADER: the Cauchy-Kovalevskaya kernel is built for 3-D degrees up to 7 (all degrees in 2-D)");
   cudaError_t e = k.launch(a, c->grid_ck, c->stream);
   ++c->launches;
   if (e != cudaSuccess) return cuda_fail(c, e, "ck kernel launch");
@@ -988,6 +987,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   c->cart = cart;
   c->post = opt.use_ader_post != 0;
   c->kt = &ew::kernel_table(c->dim, c->np);
+  c->line = cart && c->kt->cart[ew::CV_F64_MID].launch != nullptr;
   const int dim = c->dim, nv = 1 << dim;
 
   auto bail = [&](int code) {
@@ -1133,10 +1133,9 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   // mixed CK kernel: 80 registers a thread, two blocks per SM need 384 threads or fewer
   c->cb_ck = c->mixed && !c->ff ? std::max(1, std::min(c->cb_stage, 384 / c->N)) : c->cb_stage;
   const int ck_var = c->ff ? 2 : (c->mixed ? 1 : 0);
-  while (c->cb_ck > 1 &&
-         c->kt->ck[ck_var][cart][c->post].smem(c->cb_ck) > 200 * 1024)
-    --c->cb_ck;
-  if (cart) {
+  const ew::KernelEntry& ckk = c->kt->ck[ck_var][cart][c->post];
+  while (ckk.smem && c->cb_ck > 1 && ckk.smem(c->cb_ck) > 200 * 1024) --c->cb_ck;
+  if (c->line) {
     const int lines = c->kt->lines;
     const int tuned = ew::tuned_cells_per_block(c->dim, c->degree, opt.precision);
     c->cb_cart = opt.cells_per_block > 0 ? opt.cells_per_block
@@ -1147,15 +1146,15 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   }
   if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
       (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)) ||
-      (cart && (rc = build_work(c, c->cb_cart, &c->d_work_cart, &c->n_work_cart))))
+      (c->line && (rc = build_work(c, c->cb_cart, &c->d_work_cart, &c->n_work_cart))))
     return bail(rc);
   for (int v = 0; v < ew::N_STAGE_VARIANTS; ++v) {
     if (!c->kt->stage[v][cart].occupancy) continue;  // compensated variants: curved cells only
     const int occ = c->kt->stage[v][cart].occupancy(c->cb_stage);
     c->grid_stage[v] = std::max(1, std::min(c->n_work_stage, std::max(occ, 1) * c->num_sms));
   }
-  {
-    const int occ = c->kt->ck[ck_var][cart][c->post].occupancy(c->cb_ck);
+  if (ckk.occupancy) {
+    const int occ = ckk.occupancy(c->cb_ck);
     c->grid_ck = std::max(1, std::min(c->n_work_ck, std::max(occ, 1) * c->num_sms));
   }
   // integrator scratch: FP64 third register (also the ADER Taylor state);
@@ -1408,7 +1407,47 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
                ? EW_OK
                : fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
   using namespace ew;
-  if (!ctx->mixed || !ctx->cart || ctx->ff) {
+  if (ctx->ff && ctx->line) {
+    // Compensated, Cartesian.  Between two steps the state is kept as float
+    // pairs (8 bytes, like FP64): the last stage of every step but the call's
+    // final one writes the pairs in place of its accumulator, and the next
+    // step's first stage reads them as its input and accumulator at once, with
+    // its own accumulator in the other vector.  State and accumulator trade
+    // vectors every step; the call's final step writes FP64.
+    const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
+    const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt,
+                          (kB4 - kA54) * dt, 0.0};
+    float* xb[2] = {ctx->d_x32[0], ctx->d_x32[1]};
+    double* st = vec_n;   // state: FP64 before the first step, float pairs after
+    double* ac = vec_np;  // accumulator of the current step
+    for (int64_t step = 0; step < n_steps; ++step) {
+      const bool last_step = step + 1 == n_steps;
+      if (step == 0)
+        rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, st, st, xb[0], ac, MODE_RK_MID, f1[0],
+                          f2[0], 1.0f);
+      else
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, st, st, xb[0], ac, MODE_RK_MID, f1[0],
+                          f2[0], 1.0f);
+      if (rc) return rc;
+      int cur = 0;
+      for (int s = 1; s < 4; ++s) {
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, ac, xb[cur], xb[cur ^ 1], ac, MODE_RK_MID,
+                          f1[s], f2[s], 1.0f);
+        if (rc) return rc;
+        cur ^= 1;
+      }
+      rc = launch_stage(ctx, STAGE_MIX_IN32, last_step ? CV_MIX_LAST : CV_FF_LAST_PAIR, ac, xb[cur],
+                        nullptr, ac, MODE_RK_LAST, f1[4], f2[4], 1.0f);
+      if (rc) return rc;
+      std::swap(st, ac);
+    }
+    if (st != vec_np &&
+        cudaMemcpyAsync(vec_np, st, (size_t)ctx->n_dofs * sizeof(double), cudaMemcpyDeviceToDevice,
+                        ctx->stream) != cudaSuccess)
+      return fail(ctx, EW_ERR_CUDA, "ew_lsrk45_steps: copy");
+    return EW_OK;
+  }
+  if (!ctx->mixed || !ctx->line) {
     // one step at a time; the state alternates between the two vectors
     double* a = vec_n;
     double* b = vec_np;
@@ -1765,6 +1804,9 @@ int ew_l2_error_post_membrane(ew_ctx* ctx, const double* state, int32_t n_modes,
   const int dim = ctx->dim, np = ctx->np, m = np + 1, me = m + 1;
   int Mp = 1;
   for (int d = 0; d < dim; ++d) Mp *= m;
+  if (Mp > 1024)
+    return fail(ctx, EW_ERR_UNSUPPORTED,
+                "ew_l2_error_post_membrane: one thread per QGauss(k+2) point, at most 1024 (3-D degree <= 8)");
   if (!ctx->d_post) {
     // interp (m x np), qx, qw, D (m x m), Ie (me x m), ex, ew
     const ew::GaussRule g = ew::gauss_rule(np), gp = ew::gauss_rule(m), ge = ew::gauss_rule(me);

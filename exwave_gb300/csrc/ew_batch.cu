@@ -628,6 +628,8 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   int rc = ew::validate_mesh(&sd->mesh, &cart, &err);
   if (rc) return bfail(b, rc, err);
   if (!cart) return bfail(b, EW_ERR_UNSUPPORTED, "batched solves need Cartesian (axis-aligned) cells");
+  if (!ew::kernel_table(sd->mesh.dim, sd->mesh.degree + 1).cart[ew::CV_F64_MID].launch)
+    return bfail(b, EW_ERR_UNSUPPORTED, "batched solves: the line kernel is built for 3-D degrees up to 7");
   if (!(sd->dt > 0.0) || sd->n_steps < 1) return bfail(b, EW_ERR_INVALID, "dt and n_steps must be positive");
   if (sd->n_sources < 0 || sd->n_sources > 1 || sd->n_receivers < 0 || sd->n_receivers > 64 ||
       (sd->n_receivers > 0 && !sd->receivers))

@@ -59,27 +59,31 @@ __device__ __forceinline__ R end_sum(R v) {
 // for i < H = NP/2, a_i = sum_j P_ij e_j (+ mid_col_i x_m), b_i = sum_j Q_ij o_j,
 // y_i = a_i + b_i, y_{n-1-i} = b_i - a_i, and for odd NP y_m = sum_j mid_row_j o_j,
 // with e_j = x_j + x_{n-1-j}, o_j = x_j - x_{n-1-j}.
+// Sizes for up to 13 points per line (degree 12): H = NP / 2 <= 6.
+constexpr int kEoMax = 6;
+constexpr int kLineMax = 16;
+
 template <typename Real>
 struct EoMat {
-  Real P[4][4], Q[4][4];
-  Real mid_row[4], mid_col[4];
+  Real P[kEoMax][kEoMax], Q[kEoMax][kEoMax];
+  Real mid_row[kEoMax], mid_col[kEoMax];
 };
 
 template <typename Real>
 struct CartBasis {
   EoMat<Real> D;   // D[i][j] = l_j'(x_i)
   EoMat<Real> Dt;  // Dt[i][a] = D[a][i] w_a / w_i
-  Real Ls[4], La[4], Lmid;  // traces: t0 = s + a, t1 = s - a
-  Real Ws[4], Wa[4], Wmid;  // lifts with l_j(s)/w_j
-  Real L[2][8];             // l_j(0), l_j(1) (neighbour traces)
+  Real Ls[kEoMax], La[kEoMax], Lmid;  // traces: t0 = s + a, t1 = s - a
+  Real Ws[kEoMax], Wa[kEoMax], Wmid;  // lifts with l_j(s)/w_j
+  Real L[2][kLineMax];                // l_j(0), l_j(1) (neighbour traces)
 };
 
 // Host-side construction from the 1D Gauss data.
 inline void make_eo(const double* M, int NP, EoMat<double>& E) {
   const int H = NP / 2;
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) E.P[i][j] = E.Q[i][j] = 0.0;
-  for (int i = 0; i < 4; ++i) E.mid_row[i] = E.mid_col[i] = 0.0;
+  for (int i = 0; i < kEoMax; ++i)
+    for (int j = 0; j < kEoMax; ++j) E.P[i][j] = E.Q[i][j] = 0.0;
+  for (int i = 0; i < kEoMax; ++i) E.mid_row[i] = E.mid_col[i] = 0.0;
   for (int i = 0; i < H; ++i)
     for (int j = 0; j < H; ++j) {
       E.P[i][j] = 0.5 * (M[i * NP + j] + M[i * NP + NP - 1 - j]);
@@ -142,10 +146,10 @@ struct CartConst<FF> {
 // kernel: every anchored line sum (ew_ff.cuh) takes its anchor from
 // sum_j |c_j| |x_j| of its own terms, computed with these.
 struct FfBounds {
-  float aDP[4][4], aDQ[4][4], aDmc[4], aDmr[4];
-  float aTP[4][4], aTQ[4][4], aTmc[4], aTmr[4];
-  float aWs[4], aWa[4], aWmid;
-  float aLs[4], aLa[4], aLmid, aL[2][8];
+  float aDP[kEoMax][kEoMax], aDQ[kEoMax][kEoMax], aDmc[kEoMax], aDmr[kEoMax];
+  float aTP[kEoMax][kEoMax], aTQ[kEoMax][kEoMax], aTmc[kEoMax], aTmr[kEoMax];
+  float aWs[kEoMax], aWa[kEoMax], aWmid;
+  float aLs[kEoMax], aLa[kEoMax], aLmid, aL[2][kLineMax];
 };
 namespace {
 __constant__ FfBounds c_ff_bounds;
@@ -157,7 +161,7 @@ inline CartBasis<double> make_cart_basis(int NP, const double* w, const double* 
   CartBasis<double> c;
   std::memset(&c, 0, sizeof(c));
   make_eo(D, NP, c.D);
-  double Dt[64];
+  double Dt[kLineMax * kLineMax];
   for (int i = 0; i < NP; ++i)
     for (int a = 0; a < NP; ++a) Dt[i * NP + a] = D[a * NP + i] * w[a] / w[i];
   make_eo(Dt, NP, c.Dt);
@@ -182,8 +186,8 @@ inline CartBasis<double> make_cart_basis(int NP, const double* w, const double* 
 
 inline FfBounds make_ff_bounds(const CartBasis<double>& c) {
   FfBounds f;
-  for (int i = 0; i < 4; ++i) {
-    for (int j = 0; j < 4; ++j) {
+  for (int i = 0; i < kEoMax; ++i) {
+    for (int j = 0; j < kEoMax; ++j) {
       f.aDP[i][j] = std::fabs((float)c.D.P[i][j]);
       f.aDQ[i][j] = std::fabs((float)c.D.Q[i][j]);
       f.aTP[i][j] = std::fabs((float)c.Dt.P[i][j]);
@@ -197,12 +201,12 @@ inline FfBounds make_ff_bounds(const CartBasis<double>& c) {
     f.aWa[i] = std::fabs((float)c.Wa[i]);
   }
   f.aWmid = std::fabs((float)c.Wmid);
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < kEoMax; ++j) {
     f.aLs[j] = std::fabs((float)c.Ls[j]);
     f.aLa[j] = std::fabs((float)c.La[j]);
   }
   f.aLmid = std::fabs((float)c.Lmid);
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < kLineMax; ++j) {
     f.aL[0][j] = std::fabs((float)c.L[0][j]);
     f.aL[1][j] = std::fabs((float)c.L[1][j]);
   }
@@ -361,6 +365,11 @@ struct CartSmem {
 //                place of A)
 //  MIX_LAST_FF : last stage of such a step: the new state is left as that
 //                pair, hi to Xout and lo to Aout (no rounding to FP64)
+//  FF_LAST_PAIR: compensated operator, last stage of a step inside a
+//                multi-step call: the new state is written as float pairs
+//                (8 bytes, like the FP64 value it stands for) to Aout; the
+//                next step's first stage reads it like a middle stage reads
+//                its input and accumulator (X == A)
 // Within an LSRK step the mixed path keeps the accumulator as an unevaluated
 // sum hi + lo of two floats (about 48 significant bits) in the 8-byte slot
 // of the FP64 vector, updated with error-free transformations on the FP32
@@ -374,7 +383,8 @@ enum Epi : int {
   EPI_MIX_LAST = 5,
   EPI_MIX_UPD = 6,
   EPI_MIX_S1_FF = 7,
-  EPI_MIX_LAST_FF = 8
+  EPI_MIX_LAST_FF = 8,
+  EPI_FF_LAST_PAIR = 9
 };
 
 template <int EPI>
@@ -425,7 +435,7 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     // compensated operator: the update of the float-pair accumulator in FF
     // arithmetic too (the mixed path rounds the increment to FP32)
     static_assert(EPI == EPI_APPLY || EPI == EPI_MIX_S1 || EPI == EPI_MIX_MID || EPI == EPI_MIX_LAST ||
-                      EPI == EPI_MIX_UPD,
+                      EPI == EPI_MIX_UPD || EPI == EPI_FF_LAST_PAIR,
                   "FF epilogues: apply, LSRK stages 1, middle and 5, ADER update");
     if constexpr (EPI == EPI_APPLY) {
       an = real_to_f64<Real>(k);
@@ -436,6 +446,9 @@ __device__ __forceinline__ void epi_value(const SolveDesc& sd, double a, Real k,
     } else if constexpr (EPI == EPI_MIX_LAST) {
       const FF r = FF(ff_hi(a), ff_lo(a)) + FF(sd.f1_hi, sd.f1_lo) * k;
       an = f32_to_f64(r.hi) + f32_to_f64(r.lo);
+    } else if constexpr (EPI == EPI_FF_LAST_PAIR) {
+      const FF r = FF(ff_hi(a), ff_lo(a)) + FF(sd.f1_hi, sd.f1_lo) * k;
+      an = ff_pack(r.hi, r.lo);
     } else {
       const FF acc(ff_hi(a), ff_lo(a));
       xn = acc + FF(sd.f1_hi, sd.f1_lo) * k;
@@ -500,6 +513,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
   constexpr int F = DIM + 1;
   constexpr int NL = ipow_c(NP, DIM - 1);
   constexpr int H = NP / 2;
+  constexpr int HA = H > 0 ? H : 1;  // array extent of the even-odd halves
   constexpr bool CONV = !is_f64_v<Real> && is_f64_v<InT>;
   constexpr bool LO_IN = EpiTraits<EPI>::lo_in;
   constexpr bool LO_OUT = EpiTraits<EPI>::lo_out;
@@ -799,7 +813,11 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
     // ---------------------------------------------------------- line phase
     // stage input values as Real, from the X buffer or (X == A) the A buffer
     auto xval = [&](int idx) -> Real {
-      if constexpr (sizeof(InT) == 4 || is_ff_v<InT>) {
+      if constexpr (is_ff_v<InT>) {
+        // float pairs: staged on their own, or (X == A, the first stage of a
+        // step from a float-pair state) in the accumulator's buffer
+        return stage_x ? sX[idx] : reinterpret_cast<const FF*>(sA)[idx];
+      } else if constexpr (sizeof(InT) == 4) {
         return sX[idx];
       } else if constexpr (CONV && is_ff_v<Real>) {
         const float* p = reinterpret_cast<const float*>(stage_x ? static_cast<const void*>(sX)
@@ -837,7 +855,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
             xu[j] = xval(xo + e * N + base + j * str);
             xp[j] = xval(xo + DIM * N + base + j * str);
           }
-          FF eu[4], ou[4], ep[4], op[4];
+          FF eu[HA], ou[HA], ep[HA], op[HA];
 #pragma unroll
           for (int j = 0; j < H; ++j) {
             eu[j] = ffu_add(xu[j], xu[NP - 1 - j]);
@@ -966,10 +984,10 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
           // Each output pair (a_i, b_i) gets its own anchor from the row's
           // sum of |coefficient| |value| (float parts), which keeps the
           // anchor within a factor 4 of the row's largest partial sum.
-          auto contract = [&](const EoMat<FF>& M, const float (*aP)[4], const float (*aQ)[4],
+          auto contract = [&](const EoMat<FF>& M, const float (*aP)[kEoMax], const float (*aQ)[kEoMax],
                               const float* amc, const float* amr, const FF* ev, const FF* ov, FF xm,
                               FF Gs, FF Gd, FF c, FF* k) {
-            float ae[4], ao[4];
+            float ae[HA], ao[HA];
 #pragma unroll
             for (int j = 0; j < H; ++j) {
               ae[j] = fabsf(ev[j].hi);
@@ -1022,7 +1040,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
             xu[j] = xval(xo + e * N + base + j * str);
             xp[j] = xval(xo + DIM * N + base + j * str);
           }
-          Real eu[4], ou[4], ep[4], op[4];
+          Real eu[HA], ou[HA], ep[HA], op[HA];
 #pragma unroll
           for (int j = 0; j < H; ++j) {
             eu[j] = xu[j] + xu[NP - 1 - j];
@@ -1118,7 +1136,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
             Fp[s] = rc2 * (-un_p + tau_p * (lambda - tp[s]));
           }
           // derivative of p and weighted transpose derivative of u_e
-          Real a1[4 + 1], b1[4], a2[4 + 1], b2[4];
+          Real a1[HA + 1], b1[HA], a2[HA + 1], b2[HA];
           eo_apply<NP, Real>(B.D, ep, op, pm, a1, b1);
           eo_apply<NP, Real>(B.Dt, eu, ou, um, a2, b2);
           const Real Fsu = Fu[0] + Fu[1], Fdu = Fu[0] - Fu[1];

@@ -93,9 +93,9 @@ struct LaunchArgs {
   // ADER Taylor coefficients, prepared on the host: dt, dt^2/2 and for the
   // recursive derivative j = s + 2 the factor -1/2 prod_{i=2}^{s+2}(-1/(i+1)) dt^(s+3)
   float ck_dt, ck_half_dt2;
-  float ck_fac[8];
+  float ck_fac[12];
   double ck_dt_d, ck_half_dt2_d;
-  double ck_fac_d[8];
+  double ck_fac_d[12];
 };
 
 // ---------------------------------------------------------------- basis table

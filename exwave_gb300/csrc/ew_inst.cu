@@ -19,6 +19,16 @@ namespace {
 constexpr int DIM = EW_DIM;
 constexpr int NP = EW_NP;
 constexpr int N = ipow_c(NP, DIM);
+// The line kernel and the CK kernel keep whole cells in shared memory; in
+// 3-D beyond 9^3 points (degree 8 and above) they do not fit, and those
+// degrees run the generic stage kernel only (several points per thread).
+constexpr bool LINE_OK = DIM == 2 || NP <= 8;
+constexpr bool CK_OK = DIM == 2 || NP <= 8;
+// threads of the generic stage kernel: one per point, or a cell of more
+// than 512 points spread over PPT points per thread (one cell per block)
+constexpr int STAGE_PPT = (N + 511) / 512;
+constexpr int STAGE_THREADS_1 = ((N + STAGE_PPT - 1) / STAGE_PPT + 31) / 32 * 32;
+inline int stage_threads(int cb) { return STAGE_PPT > 1 ? STAGE_THREADS_1 : cb * N; }
 
 // Prefer the largest shared-memory carve-out: the kernels are limited by
 // resident CTAs, not by L1 hits.
@@ -58,7 +68,7 @@ struct StageK {
   // 16 bytes; the pointers are checked at launch.
   static bool staged_ok(int cb) {
     constexpr size_t F = DIM + 1;
-    return !CART && std::is_same<Real, InT>::value && (F * N * sizeof(Real)) % 16 == 0 &&
+    return !CART && std::is_same<Real, InT>::value && N <= 512 && (F * N * sizeof(Real)) % 16 == 0 &&
            (F * N * 8) % 16 == 0 && ((size_t)(1 << DIM) * DIM * sizeof(Real)) % 16 == 0 &&
            2 * DIM <= N && smem_staged(cb) <= 220 * 1024;
   }
@@ -71,14 +81,14 @@ struct StageK {
           (s.mode == MODE_APPLY || aligned(s.A)))
         return run(stage_kernel_staged<DIM, NP, Real, OutT>, a, grid, cb * N, smem_staged(cb), st);
     }
-    return run(stage_kernel<DIM, NP, Real, InT, OutT, CART>, a, grid, cb * N, smem(cb), st);
+    return run(stage_kernel<DIM, NP, Real, InT, OutT, CART>, a, grid, stage_threads(cb), smem(cb), st);
   }
   static int occupancy(int cb) {
     if constexpr (!CART && std::is_same<Real, InT>::value) {
       if (staged_ok(cb))
         return blocks_per_sm(stage_kernel_staged<DIM, NP, Real, OutT>, cb * N, smem_staged(cb));
     }
-    return blocks_per_sm(stage_kernel<DIM, NP, Real, InT, OutT, CART>, cb * N, smem(cb));
+    return blocks_per_sm(stage_kernel<DIM, NP, Real, InT, OutT, CART>, stage_threads(cb), smem(cb));
   }
 };
 
@@ -162,23 +172,26 @@ void EW_TABLE_FN(KernelTable& t) {
   t.points = N;
   t.lines = DIM * ipow_c(NP, DIM - 1);
   t.set_constants = &set_constants;
-  fill_cart<CartK<double, double, EPI_APPLY>>(t.cart[CV_F64_APPLY]);
-  fill_cart<CartK<double, double, EPI_F64_MID>>(t.cart[CV_F64_MID]);
-  fill_cart<CartK<double, double, EPI_F64_LAST>>(t.cart[CV_F64_LAST]);
-  fill_cart<CartK<float, double, EPI_APPLY>>(t.cart[CV_MIX_APPLY64]);
-  fill_cart<CartK<float, double, EPI_MIX_S1>>(t.cart[CV_MIX_S1]);
-  fill_cart<CartK<float, float, EPI_APPLY>>(t.cart[CV_MIX_APPLY32]);
-  fill_cart<CartK<float, float, EPI_MIX_MID>>(t.cart[CV_MIX_MID]);
-  fill_cart<CartK<float, float, EPI_MIX_LAST>>(t.cart[CV_MIX_LAST]);
-  fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
-  fill_cart<CartK<float, float, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
-  fill_cart<CartK<float, float, EPI_MIX_LAST_FF>>(t.cart[CV_MIX_LAST_FF]);
-  fill_cart<CartK<FF, double, EPI_APPLY>>(t.cart[CV_FF_APPLY64]);
-  fill_cart<CartK<FF, double, EPI_MIX_S1>>(t.cart[CV_FF_S1]);
-  fill_cart<CartK<FF, FF, EPI_MIX_MID>>(t.cart[CV_FF_MID]);
-  fill_cart<CartK<FF, FF, EPI_MIX_LAST>>(t.cart[CV_FF_LAST]);
-  fill_cart<CartK<FF, FF, EPI_MIX_UPD>>(t.cart[CV_FF_UPD]);
-  fill_cart<CartK<FF, FF, EPI_APPLY>>(t.cart[CV_FF_APPLYFF]);
+  if constexpr (LINE_OK) {
+    fill_cart<CartK<double, double, EPI_APPLY>>(t.cart[CV_F64_APPLY]);
+    fill_cart<CartK<double, double, EPI_F64_MID>>(t.cart[CV_F64_MID]);
+    fill_cart<CartK<double, double, EPI_F64_LAST>>(t.cart[CV_F64_LAST]);
+    fill_cart<CartK<float, double, EPI_APPLY>>(t.cart[CV_MIX_APPLY64]);
+    fill_cart<CartK<float, double, EPI_MIX_S1>>(t.cart[CV_MIX_S1]);
+    fill_cart<CartK<float, float, EPI_APPLY>>(t.cart[CV_MIX_APPLY32]);
+    fill_cart<CartK<float, float, EPI_MIX_MID>>(t.cart[CV_MIX_MID]);
+    fill_cart<CartK<float, float, EPI_MIX_LAST>>(t.cart[CV_MIX_LAST]);
+    fill_cart<CartK<float, float, EPI_MIX_UPD>>(t.cart[CV_MIX_UPD]);
+    fill_cart<CartK<float, float, EPI_MIX_S1_FF>>(t.cart[CV_MIX_S1_FF]);
+    fill_cart<CartK<float, float, EPI_MIX_LAST_FF>>(t.cart[CV_MIX_LAST_FF]);
+    fill_cart<CartK<FF, double, EPI_APPLY>>(t.cart[CV_FF_APPLY64]);
+    fill_cart<CartK<FF, double, EPI_MIX_S1>>(t.cart[CV_FF_S1]);
+    fill_cart<CartK<FF, FF, EPI_MIX_MID>>(t.cart[CV_FF_MID]);
+    fill_cart<CartK<FF, FF, EPI_MIX_LAST>>(t.cart[CV_FF_LAST]);
+    fill_cart<CartK<FF, FF, EPI_MIX_UPD>>(t.cart[CV_FF_UPD]);
+    fill_cart<CartK<FF, FF, EPI_APPLY>>(t.cart[CV_FF_APPLYFF]);
+    fill_cart<CartK<FF, FF, EPI_FF_LAST_PAIR>>(t.cart[CV_FF_LAST_PAIR]);
+  }
   // stage kernels: [variant][cart]
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
   fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);
@@ -186,22 +199,29 @@ void EW_TABLE_FN(KernelTable& t) {
   fill<StageK<float, double, float, true>>(t.stage[STAGE_MIX_IN64][1]);
   fill<StageK<float, float, float, false>>(t.stage[STAGE_MIX_IN32][0]);
   fill<StageK<float, float, float, true>>(t.stage[STAGE_MIX_IN32][1]);
-  // compensated: curved cells only (axis-aligned cells use the line kernel)
+  // compensated: curved cells (axis-aligned cells use the line kernel where it is built)
   fill<StageK<FF, double, FF, false>>(t.stage[STAGE_FF_IN64][0]);
   fill<StageK<FF, FF, FF, false>>(t.stage[STAGE_FF_INFF][0]);
+  if constexpr (!LINE_OK) {
+    // axis-aligned cells without the line kernel
+    fill<StageK<FF, double, FF, true>>(t.stage[STAGE_FF_IN64][1]);
+    fill<StageK<FF, FF, FF, true>>(t.stage[STAGE_FF_INFF][1]);
+  }
   // CK kernels: [precision][cart][post]
-  fill<CkK<double, double, double, false, false>>(t.ck[0][0][0]);
-  fill<CkK<double, double, double, false, true>>(t.ck[0][0][1]);
-  fill<CkK<double, double, double, true, false>>(t.ck[0][1][0]);
-  fill<CkK<double, double, double, true, true>>(t.ck[0][1][1]);
-  fill<CkK<float, double, float, false, false>>(t.ck[1][0][0]);
-  fill<CkK<float, double, float, false, true>>(t.ck[1][0][1]);
-  fill<CkK<float, double, float, true, false>>(t.ck[1][1][0]);
-  fill<CkK<float, double, float, true, true>>(t.ck[1][1][1]);
-  fill<CkK<FF, double, FF, false, false>>(t.ck[2][0][0]);
-  fill<CkK<FF, double, FF, false, true>>(t.ck[2][0][1]);
-  fill<CkK<FF, double, FF, true, false>>(t.ck[2][1][0]);
-  fill<CkK<FF, double, FF, true, true>>(t.ck[2][1][1]);
+  if constexpr (CK_OK) {
+    fill<CkK<double, double, double, false, false>>(t.ck[0][0][0]);
+    fill<CkK<double, double, double, false, true>>(t.ck[0][0][1]);
+    fill<CkK<double, double, double, true, false>>(t.ck[0][1][0]);
+    fill<CkK<double, double, double, true, true>>(t.ck[0][1][1]);
+    fill<CkK<float, double, float, false, false>>(t.ck[1][0][0]);
+    fill<CkK<float, double, float, false, true>>(t.ck[1][0][1]);
+    fill<CkK<float, double, float, true, false>>(t.ck[1][1][0]);
+    fill<CkK<float, double, float, true, true>>(t.ck[1][1][1]);
+    fill<CkK<FF, double, FF, false, false>>(t.ck[2][0][0]);
+    fill<CkK<FF, double, FF, false, true>>(t.ck[2][0][1]);
+    fill<CkK<FF, double, FF, true, false>>(t.ck[2][1][0]);
+    fill<CkK<FF, double, FF, true, true>>(t.ck[2][1][1]);
+  }
 }
 
 }  // namespace ew

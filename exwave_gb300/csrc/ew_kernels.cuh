@@ -385,7 +385,10 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
   Real* sFl = sm + lay.Fl;
   Real* sGeo = sm + lay.geo;
   Real* sMat = sm + lay.mat;
-  if ((int)blockDim.x != CB * N) {
+  // points per thread: one (CB cells of at most 512 points each), or, for a
+  // cell of more points (3-D, degree 8 and above), several, one cell per block
+  constexpr int PPT = (N + 511) / 512;
+  if ((int)blockDim.x * PPT < CB * N || (PPT > 1 && CB != 1)) {
     if (threadIdx.x == 0) atomicOr(La.err, ERR_BAD_LAUNCH);
     return;
   }
@@ -399,19 +402,27 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
     load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
     __syncthreads();
     const Real bf = static_cast<Real>(sd.bf);
-    const int cl = threadIdx.x / N;
-    const int q = threadIdx.x - cl * N;
-    const bool active = cl < nc;
-    Real Ru[DIM];
-    Real inv_jxw = Real(1);
-    if (active) op_cell<DIM, NP, Real, CART>(sB, sX, sG, sGeo, sMat, cl, q, bf, Ru, inv_jxw);
+    Real Ru[PPT][DIM];
+    Real inv_jxw[PPT];
+#pragma unroll
+    for (int r = 0; r < PPT; ++r) {
+      const int idx = threadIdx.x + r * blockDim.x;
+      const int cl = idx / N;
+      inv_jxw[r] = Real(1);
+      if (cl < nc) op_cell<DIM, NP, Real, CART>(sB, sX, sG, sGeo, sMat, cl, idx - cl * N, bf, Ru[r], inv_jxw[r]);
+    }
     for (int fp = threadIdx.x; fp < nc * 2 * DIM * S::NF; fp += blockDim.x)
       op_face<DIM, NP, Real, InT, CART>(sB, sX, sFl, sGeo, sMat, sd, wi.cell_begin, nc, fp, bf,
                                         La.err);
     __syncthreads();
-    if (!active) continue;
+#pragma unroll
+    for (int r = 0; r < PPT; ++r) {
+    const int idx = threadIdx.x + r * blockDim.x;
+    const int cl = idx / N;
+    const int q = idx - cl * N;
+    if (cl >= nc) continue;
     Real k[F];
-    op_collect<DIM, NP, Real, CART>(sB, sG, sFl, cl, q, Ru, inv_jxw, k);
+    op_collect<DIM, NP, Real, CART>(sB, sG, sFl, cl, q, Ru[r], inv_jxw[r], k);
 
     const size_t g0 = ((size_t)wi.cell_begin + cl) * F * N + q;
     const int mode = sd.mode;
@@ -461,6 +472,7 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
         }
       }
     }
+    }  // points of this thread
   }
 }
 
@@ -703,9 +715,9 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     return;
   }
   load_basis<Real>(La.basis, sB, basis_total(NP));
-  Real fac[8];
+  Real fac[12];
 #pragma unroll
-  for (int s = 0; s < 8; ++s) {
+  for (int s = 0; s < 12; ++s) {
     if constexpr (is_f64_v<Real>)
       fac[s] = La.ck_fac_d[s];
     else if constexpr (is_ff_v<Real>)

@@ -44,7 +44,8 @@ enum CartVariant : int {
   CV_FF_LAST = 14,      // compensated LSRK stage 5 (FP64 state out)
   CV_FF_UPD = 15,       // compensated ADER update u + M^-1 A(T), T as float pairs
   CV_FF_APPLYFF = 16,   // compensated operator on a float-pair input
-  N_CART_VARIANTS = 17
+  CV_FF_LAST_PAIR = 17, // compensated LSRK stage 5, state left as float pairs (multi-step calls)
+  N_CART_VARIANTS = 18
 };
 
 // Launcher of the Cartesian line kernel.
@@ -67,7 +68,9 @@ struct KernelTable {
 
 #define EW_DECL(d, n) void kernel_table_d##d##_##n(KernelTable&);
 EW_DECL(2, 2) EW_DECL(2, 3) EW_DECL(2, 4) EW_DECL(2, 5) EW_DECL(2, 6) EW_DECL(2, 7) EW_DECL(2, 8)
+EW_DECL(2, 9) EW_DECL(2, 10) EW_DECL(2, 11) EW_DECL(2, 12) EW_DECL(2, 13)
 EW_DECL(3, 2) EW_DECL(3, 3) EW_DECL(3, 4) EW_DECL(3, 5) EW_DECL(3, 6) EW_DECL(3, 7) EW_DECL(3, 8)
+EW_DECL(3, 9) EW_DECL(3, 10) EW_DECL(3, 11) EW_DECL(3, 12) EW_DECL(3, 13)
 #undef EW_DECL
 
 }  // namespace ew

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define EW_MAX_DEGREE 7 /* k = 1..7 (the reference instantiates 1..12) */
+#define EW_MAX_DEGREE 12 /* k = 1..12, as the reference instantiates */
 
 typedef enum ew_status {
   EW_OK = 0,

@@ -58,8 +58,8 @@ def _create(lib, mesh, degree):
 def test_create_rejects_bad_meshes(lib):
     import exwave_gb300 as ew
     m = ew.hypercube(2, 3)
-    rc, msg = _create(lib, m, 8)
-    assert rc == -2 and "degree" in msg
+    rc, msg = _create(lib, m, 13)     # the reference instantiates k = 1..12
+    assert rc == -1 and "degree" in msg
     rc, msg = _create(lib, m, 0)
     assert rc == -1
     bad = ew.hypercube(2, 3)

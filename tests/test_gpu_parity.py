@@ -104,7 +104,7 @@ def test_lsrk45_steps(env, case):
 
 
 @pytest.mark.parametrize("case", [CASES[i] for i in (1, 2, 3, 8, 11)], ids=ids)
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_ff"])
 @pytest.mark.parametrize("n_steps", [1, 2, 5])
 def test_lsrk45_steps_call(env, case, precision, n_steps):
     """ew_lsrk45_steps against n_steps calls of ew_lsrk45_step and the FP64
@@ -113,7 +113,10 @@ def test_lsrk45_steps_call(env, case, precision, n_steps):
     single-step path would round to) and runs other kernel instantiations,
     whose FP32 operations may round differently; the two paths then agree to
     FP32 round-off (1e-6 relative after 5 steps) and stay as close to the
-    FP64 oracle as the single-step path."""
+    FP64 oracle as the single-step path.  Compensated: on Cartesian meshes the
+    call keeps the state as float pairs between its steps, where single steps
+    round it to FP64 and split it again; the two agree to 1e-13 relative and
+    both equal the oracle to the compensated tolerance."""
     ew, oracle, torch = env
     dim, k, n, ref, f, bids, het = case
     m = make_case(ew, dim, n, ref, f, bids, het, seed=3)
@@ -133,6 +136,14 @@ def test_lsrk45_steps_call(env, case, precision, n_steps):
     scale = np.abs(single).max()
     if precision == "fp64":
         assert np.array_equal(multi, single)
+        return
+    if precision == "mixed_ff":
+        assert np.abs(multi - single).max() / scale < 1e-13
+        x, y = u0h.copy(), np.zeros_like(u0h)
+        for _ in range(n_steps):
+            o.lsrk45_step(dt, x, y)
+            x, y = y, x
+        assert np.abs(multi - x).max() / scale < FF_TOL
         return
     assert np.abs(multi - single).max() / scale < 1e-6
     x, y = u0h.copy(), np.zeros_like(u0h)
