@@ -71,7 +71,9 @@ def parse():
                          "(curved two-layer ADER), batch (512 independent solves), serve "
                          "(continuous batching), sweep (degrees)")
     ap.add_argument("--solves", type=int, default=512)
-    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--rates", default="0.5,2,50", help="serve: offered Poisson rates (solves/s)")
+    ap.add_argument("--trace-sample", type=int, default=6,
+                    help="serve: completed solves replayed on the FP64 path per run")
     ap.add_argument("--time-limit", type=float, default=60.0)
     ap.add_argument("--degrees", default="3,7", help="batch: degree range (inclusive)")
     ap.add_argument("--sizes", default="8,32", help="batch: cells per direction range (inclusive)")
@@ -501,16 +503,52 @@ def batch_workload(args, torch):
 
 
 def serve_workload(args, torch):
+    """Serving (continuous batching) at each offered Poisson rate of --rates,
+    for the FP32-operator and the compensated precision (or the one given by
+    --precision): solves/s, latency p50 / p99 and the backlog over a run of
+    --time-limit seconds per rate.  Then the configuration's accuracy
+    criterion: the --trace-sample cheapest completed solves of each run are
+    replayed alone on the FP64 path, and their receiver traces compared
+    (largest difference over the FP64 trace's largest value)."""
+    import numpy as np
     from exwave_gb300 import serve
-    reqs = serve.draw_requests(args.solves if args.solves != 512 else 20000, rate=args.rate,
-                               seed=11)
-    srv = serve.Server(precision=args.precision, hbm_budget_bytes=150 << 30, steps_per_tick=4)
-    stats = srv.run(reqs, time_limit=args.time_limit)
-    return {"metric": "solves/s", "value": stats["solves_per_s"], "unit": "solves/s",
-            "latency_p50_s": stats["latency_p50_s"], "latency_p99_s": stats["latency_p99_s"],
-            "stats": stats, "config": {"workload": "serving, Poisson %.0f/s, T ~ U[0.2,2], "
-                                                   "150 GB budget, %d requests, %g s limit"
-                                                   % (args.rate, len(reqs), args.time_limit)}}
+    from exwave_gb300.batch import Batch
+    rates = [float(x) for x in args.rates.split(",")]
+    precs = ["mixed", "mixed_ff"] if args.precision == "auto" else [args.precision]
+    n_req = args.solves if args.solves != 512 else 20000
+    runs = []
+    for prec in precs:
+        for rate in rates:
+            reqs = serve.draw_requests(n_req, rate=rate, seed=11)
+            srv = serve.Server(precision=prec, hbm_budget_bytes=150 << 30, steps_per_tick=4)
+            stats = srv.run(reqs, time_limit=args.time_limit)
+            srv.batch.close()
+            done = [r for r in reqs if r.finished is not None and r.rejected is None]
+            sample = sorted(done, key=lambda r: r.dofs() * r.n_steps)[:args.trace_sample]
+            errs = []
+            if sample:
+                ref = Batch(precision="fp64", hbm_budget_bytes=16 << 30, allow_overrun=True)
+                ids = [ref.add(r.make_solve()) for r in sample]
+                ref.step(max(r.n_steps for r in sample))
+                ref.synchronize()
+                for r, sid in zip(sample, ids):
+                    t64 = ref.receivers(sid)
+                    got = np.concatenate(r.trace, axis=0)
+                    errs.append(float(np.abs(got - t64).max() / max(np.abs(t64).max(), 1e-300)))
+                ref.close()
+            stats.pop("failures", None)
+            runs.append({"precision": prec, "offered_rate_per_s": rate, "stats": stats,
+                         "trace_rel_err_vs_fp64": max(errs) if errs else None,
+                         "trace_rel_err_vs_fp64_median": float(np.median(errs)) if errs else None,
+                         "trace_sample": len(errs),
+                         "meets_1e-6": bool(errs and max(errs) <= 1e-6)})
+    head = runs[0]
+    return {"metric": "solves/s", "value": head["stats"]["solves_per_s"], "unit": "solves/s",
+            "latency_p50_s": head["stats"]["latency_p50_s"],
+            "latency_p99_s": head["stats"]["latency_p99_s"], "runs": runs,
+            "config": {"workload": "serving, Poisson arrivals, T ~ U[0.2,2], 150 GB budget, "
+                                   "%d requests per run, %g s per rate" % (n_req, args.time_limit),
+                       "rates_per_s": rates, "precisions": precs}}
 
 
 def sweep_workload(args, torch):
@@ -547,9 +585,9 @@ def main():
         run_reference(args)
         return
     if args.workload != "membrane3d":
-        if args.precision == "auto":
+        if args.precision == "auto" and args.workload != "serve":
             # batches: the FP32 operator (the configuration's mixed precision);
-            # serving runs its own comparison of the precisions
+            # serving compares the precisions itself
             args.precision = "mixed"
         import torch
         if dist_info()[1] != 0:

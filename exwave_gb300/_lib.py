@@ -25,11 +25,11 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_hypercube_mesh", "ew_nodal_to_gauss", "ew_gauss_to_nodal", "ew_synchronize", "ew_kernel_launches",
            "ew_batch_create", "ew_batch_destroy", "ew_batch_last_error", "ew_batch_solve_bytes",
            "ew_batch_bytes_free", "ew_batch_add", "ew_batch_remove", "ew_batch_set_state",
-           "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_receivers",
+           "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_diverged", "ew_batch_receivers",
            "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches",
            "ew_tune_set", "ew_tune_get", "ew_lsrk45_step_static", "ew_lsrk45_steps",
            "ew_set_receivers", "ew_sample_receivers", "ew_aderadconfull_step",
-           "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update"]
+           "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update", "ew_check_wait_timeout"]
 
 
 class EwError(RuntimeError):
@@ -103,6 +103,7 @@ def load():
         "ew_nodal_to_gauss": (ctypes.c_int, [i32, i32, i64, i32, dp, dp, dp]),
         "ew_gauss_to_nodal": (ctypes.c_int, [i32, i32, i64, i32, dp, dp, dp]),
         "ew_synchronize": (ctypes.c_int, [vp]),
+        "ew_check_wait_timeout": (ctypes.c_int, [vp, ctypes.c_int32]),
         "ew_kernel_launches": (i64, [vp]),
         "ew_tune_set": (ctypes.c_int, [i32, i32, i32, i32]),
         "ew_tune_get": (i32, [i32, i32, i32]),

@@ -23,7 +23,8 @@ class SolveDesc(ctypes.Structure):
 class BatchOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("hbm_budget_bytes", ctypes.c_int64), ("max_solves", ctypes.c_int32),
-                ("use_graphs", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("allow_overrun", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("blowup_limit", ctypes.c_double)]
 
 
 _SIG = {
@@ -40,6 +41,8 @@ _SIG = {
     "ew_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ew_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32,
                                      ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "ew_batch_diverged": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32)]),
     "ew_batch_receivers": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64,
                                           ctypes.c_int64, ctypes.c_void_p]),
     "ew_batch_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -106,7 +109,7 @@ class Batch:
     """Device-resident set of solves advanced together."""
 
     def __init__(self, precision="mixed", hbm_budget_bytes=8 << 30, max_solves=4096,
-                 use_graphs=True, device=0):
+                 use_graphs=True, device=0, allow_overrun=False, blowup_limit=0.0):
         self.L = _L()
         o = BatchOptions()
         o.precision = {"fp64": _lib.EW_PREC_FP64, "mixed": _lib.EW_PREC_MIXED,
@@ -115,6 +118,8 @@ class Batch:
         o.hbm_budget_bytes = int(hbm_budget_bytes)
         o.max_solves = max_solves
         o.use_graphs = int(bool(use_graphs))
+        o.allow_overrun = int(bool(allow_overrun))
+        o.blowup_limit = float(blowup_limit)
         h = ctypes.c_void_p()
         rc = self.L.ew_batch_create(ctypes.byref(o), ctypes.byref(h))
         if rc != 0:
@@ -176,6 +181,15 @@ class Batch:
         left = [b - a for a, b in (self.info(s) for s in self.solves)]
         left = [x for x in left if x > 0]
         return min(left) if left else 0
+
+    def diverged(self):
+        """Ids of the solves whose receiver samples went non-finite or past
+        the blow-up limit (waits for the batch's stream)."""
+        cap = max(1, len(self.solves))
+        ids = (ctypes.c_int32 * cap)()
+        n = ctypes.c_int32()
+        self._chk(self.L.ew_batch_diverged(self.h, ids, cap, ctypes.byref(n)))
+        return [ids[i] for i in range(n.value)]
 
     def receivers(self, sid, first=0, count=None):
         done, _ = self.info(sid)

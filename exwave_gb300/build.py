@@ -64,6 +64,7 @@ def build(jobs=None, force=False, verbose=False):
     tasks.append((os.path.join(CSRC, "ew_api.cu"), os.path.join(OBJ, "ew_api.o"), []))
     tasks.append((os.path.join(CSRC, "ew_mesh.cpp"), os.path.join(OBJ, "ew_mesh.o"), []))
     tasks.append((os.path.join(CSRC, "ew_batch.cu"), os.path.join(OBJ, "ew_batch.o"), []))
+    tasks.append((os.path.join(CSRC, "ew_diag.cu"), os.path.join(OBJ, "ew_diag.o"), []))
     todo = [t for t in tasks if force or not os.path.exists(t[1]) or os.path.getmtime(t[1]) < newest]
     jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
     if todo:

@@ -1872,4 +1872,16 @@ int ew_synchronize(ew_ctx* ctx) {
   return EW_OK;
 }
 
+int ew_check_wait_timeout(ew_ctx* ctx, int32_t polls) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (polls < 1) return fail(ctx, EW_ERR_INVALID, "ew_check_wait_timeout: polls must be positive");
+  // earlier work first, so that its flags are not mistaken for this one's
+  if ((rc = ew_synchronize(ctx))) return rc;
+  cudaError_t e = ew::launch_wait_timeout(polls, ctx->d_err, ctx->stream);
+  ++ctx->launches;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "wait time-out launch");
+  return ew_synchronize(ctx);
+}
+
 }  // extern "C"

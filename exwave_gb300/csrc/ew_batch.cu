@@ -107,14 +107,18 @@ struct Solve {
   double* rec_w = nullptr;
   int32_t* rec_cell = nullptr;
   double* trace = nullptr;
-  double* clock = nullptr;  // [0] time, [1] steps done (as double)
+  // [0] time, [1] steps taken, [2] n_steps, [3] status (1: diverged), as doubles
+  double* clock = nullptr;
   int n_rec = 0;
   int32_t src_cell = -1;
   double src_amp = 0.0, src_f0 = 0.0, src_t0 = 0.0;
 };
 
 // Receiver sampling: one block per solve, one warp per receiver; then the
-// solve's clock advances by one step.
+// solve's clock advances by one step.  Samples of steps beyond the solve's
+// n_steps (a batch that allows overrun) are not recorded.  A sample that is
+// not finite or exceeds the blow-up limit marks the solve diverged: in its
+// clock (kept across rebuilds) and in flags[solve], which the host polls.
 struct RecDesc {
   const double* U[2];  // FP64 state by parity (FP64 batches)
   const float* H[2];   // mixed: hi part by parity
@@ -125,17 +129,22 @@ struct RecDesc {
   double* trace;
   double* clock;
   double dt;
+  double limit;  // blow-up limit (0: non-finite samples only)
   int32_t n_rec, N, F, dim;
 };
 
-__global__ void receiver_kernel(const RecDesc* rd, int n, int parity) {
+__global__ void receiver_kernel(const RecDesc* rd, int n, int parity, int32_t* flags) {
   const int s = blockIdx.x;
   if (s >= n) return;
   const RecDesc r = rd[s];
   const double* state = r.U[parity];
   const float* hi = r.H[parity];
   const int64_t step = (int64_t)r.clock[1];
+  const bool record = step < (int64_t)r.clock[2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   for (int k = warp; k < r.n_rec; k += blockDim.x >> 5) {
     const int32_t cell = r.rec_cell[k];
     const size_t p0 = ((size_t)cell * r.F + r.dim) * r.N;
@@ -144,12 +153,17 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity) {
     for (int q = lane; q < r.N; q += 32)
       acc += w[q] * (r.mixed ? (double)hi[p0 + q] + (double)r.L[p0 + q] : state[p0 + q]);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) r.trace[step * r.n_rec + k] = acc;
+    if (lane == 0) {
+      if (record) r.trace[step * r.n_rec + k] = acc;
+      if (!isfinite(acc) || (r.limit > 0.0 && fabs(acc) > r.limit)) bad = 1;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     r.clock[0] += r.dt;
-    r.clock[1] = (double)(step + 1);
+    if (record) r.clock[1] = (double)(step + 1);
+    if (bad) r.clock[3] = 1.0;
+    flags[s] = r.clock[3] != 0.0 ? 1 : 0;
   }
 }
 
@@ -195,6 +209,8 @@ struct ew_batch {
   bool mixed = true;  // FP32 or float-float operator (else FP64)
   bool ff = false;    // compensated: float-float operator, FP64 state between steps
   bool use_graphs = true;
+  bool allow_overrun = false;
+  double blowup_limit = 0.0;
   int num_sms = 0;
   int max_solves = 0;
   cudaStream_t stream = nullptr;
@@ -208,6 +224,8 @@ struct ew_batch {
   std::vector<Group> groups;
   RecDesc* d_rec = nullptr;
   int n_rec_solves = 0;
+  int32_t* d_flags = nullptr;         // per receiver-table entry: diverged
+  std::vector<int32_t> rec_ids;       // solve id of each receiver-table entry
   int* d_err = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::string last_error;
@@ -234,6 +252,9 @@ void free_groups(ew_batch* b) {
   b->groups.clear();
   if (b->d_rec) cudaFree(b->d_rec);
   b->d_rec = nullptr;
+  if (b->d_flags) cudaFree(b->d_flags);
+  b->d_flags = nullptr;
+  b->rec_ids.clear();
   for (int p = 0; p < 2; ++p)
     if (b->graph[p]) {
       cudaGraphExecDestroy(b->graph[p]);
@@ -273,7 +294,7 @@ Layout solve_layout(const ew_solve_desc* s, int precision) {
   L.trace = o;
   o += al((size_t)std::max<int64_t>(s->n_steps, 1) * std::max(s->n_receivers, 1) * 8);
   L.clock = o;
-  o += al(2 * 8);
+  o += al(4 * 8);
   L.total = o;
   return L;
 }
@@ -487,16 +508,20 @@ int rebuild(ew_batch* b) {
       r.trace = s.trace;
       r.clock = s.clock;
       r.dt = s.dt;
+      r.limit = b->blowup_limit;
       r.n_rec = s.n_rec;
       r.N = s.N;
       r.F = s.F;
       r.dim = s.dim;
       rd.push_back(r);
+      b->rec_ids.push_back(id);
     }
   b->n_rec_solves = (int)rd.size();
   if (!rd.empty()) {
     if ((e = cudaMalloc(&b->d_rec, rd.size() * sizeof(RecDesc))) != cudaSuccess ||
-        (e = cudaMemcpy(b->d_rec, rd.data(), rd.size() * sizeof(RecDesc), cudaMemcpyHostToDevice)) != cudaSuccess)
+        (e = cudaMemcpy(b->d_rec, rd.data(), rd.size() * sizeof(RecDesc), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_flags, rd.size() * sizeof(int32_t))) != cudaSuccess ||
+        (e = cudaMemset(b->d_flags, 0, rd.size() * sizeof(int32_t))) != cudaSuccess)
       return bcuda(b, e, "receiver table");
   }
   b->dirty = false;
@@ -527,7 +552,8 @@ int launch_step(ew_batch* b, int p) {
     }
   }
   if (b->n_rec_solves > 0) {
-    receiver_kernel<<<b->n_rec_solves, 256, 0, b->stream>>>(b->d_rec, b->n_rec_solves, 1 - p);
+    receiver_kernel<<<b->n_rec_solves, 256, 0, b->stream>>>(b->d_rec, b->n_rec_solves, 1 - p,
+                                                            b->d_flags);
     if ((e = cudaGetLastError()) != cudaSuccess) return bcuda(b, e, "receiver launch");
     ++n;
   }
@@ -578,6 +604,8 @@ int ew_batch_create(const ew_batch_options* opt, ew_batch** out) {
   b->mixed = opt->precision != EW_PREC_FP64;
   b->ff = opt->precision == EW_PREC_MIXED_FF;
   b->use_graphs = opt->use_graphs != 0;
+  b->allow_overrun = opt->allow_overrun != 0;
+  b->blowup_limit = opt->blowup_limit > 0.0 ? opt->blowup_limit : 0.0;
   b->max_solves = opt->max_solves;
   cudaSetDevice(b->device);
   cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -773,7 +801,11 @@ int ew_batch_add(ew_batch* b, const ew_solve_desc* sd, int32_t* id) {
   // mixed: the zero state's hi and lo parts
   for (int k = 0; b->mixed && !b->ff && k < 2; ++k)
     if (e == cudaSuccess) e = cudaMemsetAsync(s.X[k], 0, (size_t)s.n_dofs * 4, b->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(s.clock, 0, 16, b->stream);
+  if (e == cudaSuccess) {
+    // time, steps taken, n_steps, status (a pageable source: staged before the call returns)
+    const double clock0[4] = {0.0, 0.0, (double)s.n_steps, 0.0};
+    e = cudaMemcpyAsync(s.clock, clock0, sizeof(clock0), cudaMemcpyHostToDevice, b->stream);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // host vectors go out of scope
   if (e != cudaSuccess) {
     b->arena.release(off, L.total);
@@ -847,7 +879,7 @@ int ew_batch_step(ew_batch* b, int32_t n_steps) {
     if (kv.second.steps_done < kv.second.n_steps)
       left = std::min(left, kv.second.n_steps - kv.second.steps_done);
   if (left == INT64_MAX) return EW_OK;  // nothing to do
-  if (n_steps > left)
+  if (n_steps > left && !b->allow_overrun)
     return bfail(b, EW_ERR_INVALID, "n_steps exceeds the steps left of an unfinished solve");
   int rc;
   if (b->dirty) {
@@ -868,7 +900,7 @@ int ew_batch_step(ew_batch* b, int32_t n_steps) {
   bool finished = false;
   for (auto& kv : b->solves)
     if (kv.second.steps_done < kv.second.n_steps) {
-      kv.second.steps_done += n_steps;
+      kv.second.steps_done = std::min(kv.second.n_steps, kv.second.steps_done + n_steps);
       kv.second.cur ^= (n_steps & 1);
       if (kv.second.steps_done >= kv.second.n_steps) finished = true;
     }
@@ -883,6 +915,21 @@ int ew_batch_info(const ew_batch* b, int32_t id, int64_t* steps_done, int64_t* n
   if (it == b->solves.end()) return EW_ERR_INVALID;
   if (steps_done) *steps_done = it->second.steps_done;
   if (n_steps) *n_steps = it->second.n_steps;
+  return EW_OK;
+}
+
+int ew_batch_diverged(ew_batch* b, int32_t* ids, int32_t capacity, int32_t* count) {
+  if (!b || !count || capacity < 0 || (capacity > 0 && !ids)) return EW_ERR_INVALID;
+  *count = 0;
+  cudaSetDevice(b->device);
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bcuda(b, e, "synchronize");
+  if (b->n_rec_solves == 0 || !b->d_flags) return EW_OK;
+  std::vector<int32_t> flags(b->n_rec_solves);
+  e = cudaMemcpy(flags.data(), b->d_flags, flags.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return bcuda(b, e, "diverged flags");
+  for (size_t i = 0; i < flags.size(); ++i)
+    if (flags[i] && *count < capacity) ids[(*count)++] = b->rec_ids[i];
   return EW_OK;
 }
 

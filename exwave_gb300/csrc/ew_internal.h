@@ -20,6 +20,10 @@ int validate_mesh(const ew_mesh_desc* m, bool* cartesian, std::string* err);
 // current device.
 cudaError_t upload_cart_constants(int dim, int np);
 
+// One block waiting on an mbarrier that nothing completes, giving up after
+// `polls` tries and raising ERR_WAIT_TIMEOUT in *err (ew_diag.cu).
+cudaError_t launch_wait_timeout(int polls, int* err, cudaStream_t stream);
+
 // Tuned cells per block for (dim, degree, precision); 0 when unset.
 int tuned_cells_per_block(int dim, int degree, int precision);
 

@@ -292,6 +292,15 @@ typedef struct ew_batch_options {
   int64_t hbm_budget_bytes; /* arena size */
   int32_t max_solves;
   int32_t use_graphs;       /* 1: capture each step as a CUDA graph */
+  /* 1: ew_batch_step may take a solve past its n_steps; the extra steps are
+   * computed but neither sampled nor counted, so that a serving tick of many
+   * steps is not cut short by the solve with the fewest steps left (its state
+   * is then no longer the one at n_steps) */
+  int32_t allow_overrun;
+  int32_t reserved;
+  /* a solve whose receiver samples become non-finite, or larger in magnitude
+   * than this (when > 0), is marked diverged: ew_batch_diverged reports it */
+  double blowup_limit;
 } ew_batch_options;
 
 /* Ricker point source added to the pressure equation:
@@ -328,9 +337,14 @@ int ew_batch_set_state(ew_batch* batch, int32_t id, const double* state);
 /* Copies a solve's current FP64 state to a caller's device buffer. */
 int ew_batch_get_state(ew_batch* batch, int32_t id, double* state);
 /* Advances every unfinished solve by n_steps (at most the smallest number
- * of steps any unfinished solve has left). */
+ * of steps any unfinished solve has left, unless allow_overrun is set). */
 int ew_batch_step(ew_batch* batch, int32_t n_steps);
 int ew_batch_info(const ew_batch* batch, int32_t id, int64_t* steps_done, int64_t* n_steps);
+/* Ids of the solves marked diverged so far (at most capacity), after the
+ * batch's stream finishes; the caller removes them.  The analogue of the
+ * reference's blow-up test (explicit_wave.cc:498-507), per solve and on the
+ * device: the receiver samples of every step are checked. */
+int ew_batch_diverged(ew_batch* batch, int32_t* ids, int32_t capacity, int32_t* count);
 /* Receiver samples [first, first + count) of a solve into host out[count][n_receivers]. */
 int ew_batch_receivers(ew_batch* batch, int32_t id, int64_t first, int64_t count, double* out);
 int ew_batch_set_stream(ew_batch* batch, void* stream);
@@ -346,6 +360,14 @@ int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision);
 
 /* Waits for the context's stream and reports a raised device error flag. */
 int ew_synchronize(ew_ctx* ctx);
+
+/* Diagnostic of the failure path of the staged kernels (no reference
+ * counterpart): one block waits on an mbarrier that nothing completes, with
+ * the same bounded wait the kernels use but a limit of `polls` tries; it
+ * gives up, raises the time-out flag and returns, with no copy in flight.
+ * Returns what ew_synchronize then reports: EW_ERR_DEVICE (flag cleared), and
+ * the context stays usable. */
+int ew_check_wait_timeout(ew_ctx* ctx, int32_t polls);
 
 /* Number of kernels this library has launched on ctx so far. */
 int64_t ew_kernel_launches(const ew_ctx* ctx);

@@ -1,8 +1,9 @@
 """The serving loop's host logic (exwave_gb300.serve.Server.run) on the CPU,
 with a fake batch in place of the device runtime: FIFO admission under an
 HBM budget (waiting while a solve does not fit), retirement at the end
-time, receiver samples read once each, latency statistics, and errors
-other than "over budget" propagated."""
+time, receiver samples read once each, latency statistics, requests that
+fail admission for a reason of their own rejected while the others are
+served, and solves the device reports diverged evicted."""
 import numpy as np
 import pytest
 
@@ -16,9 +17,12 @@ class FakeBatch:
         self.budget, self.used, self.peak = budget, 0, 0
         self.solves, self.next_id, self.admit_order = {}, 0, []
         self.fail_code = None
+        self.fail_cells = None     # only solves of this many cells fail
+        self.diverge_after = {}    # solve index -> steps after which it diverges
 
     def add(self, solve):
-        if self.fail_code is not None:
+        if self.fail_code is not None and (self.fail_cells is None or
+                                           solve.mesh.n_cells == self.fail_cells):
             raise _lib.EwError(self.fail_code, "injected")
         cost = solve.mesh.n_cells * 4 * (solve.degree + 1) ** 3
         if self.used + cost > self.budget:
@@ -45,6 +49,10 @@ class FakeBatch:
     def synchronize(self):
         pass
 
+    def diverged(self):
+        return [sid for sid, (s, d, _) in self.solves.items()
+                if sid in self.diverge_after and d >= self.diverge_after[sid]]
+
     def info(self, sid):
         s, d, _ = self.solves[sid]
         return d, s.n_steps
@@ -58,6 +66,7 @@ def _server(budget, steps_per_tick=3):
     srv = serve.Server.__new__(serve.Server)
     srv.batch = FakeBatch(budget)
     srv.steps_per_tick = steps_per_tick
+    srv.prepare_threads = 2
     return srv
 
 
@@ -85,12 +94,30 @@ def test_fifo_admission_under_budget_and_statistics():
     assert stats["peak_active"] >= 1 and stats["ticks"] >= 1
 
 
-def test_other_errors_propagate():
-    reqs = serve.draw_requests(2, rate=0.0, seed=4, cells=(2, 3), end_time=(0.02, 0.03))
+def test_admission_failure_rejects_that_request_only():
+    """An admission error of the request's own (not memory) rejects it, with
+    the error kept, and the server serves the others."""
+    reqs = serve.draw_requests(4, rate=0.0, seed=4, cells=(2, 2), end_time=(0.02, 0.03))
+    reqs[1].cells = 3
     srv = _server(budget=1 << 40)
     srv.batch.fail_code = -1
-    with pytest.raises(_lib.EwError):
-        srv.run(reqs)
+    srv.batch.fail_cells = 27
+    stats = srv.run(reqs)
+    assert stats["failed"] == 1 and stats["completed"] == 3
+    assert "injected" in reqs[1].rejected and reqs[1].finished is None
+    assert stats["failures"] == {1: reqs[1].rejected}
+
+
+def test_diverged_solve_is_evicted():
+    """A solve the device marks diverged leaves the batch with an error
+    status; the others complete."""
+    reqs = serve.draw_requests(3, rate=0.0, seed=8, cells=(2, 2), end_time=(0.05, 0.05))
+    srv = _server(budget=1 << 40, steps_per_tick=2)
+    srv.batch.diverge_after = {1: 2}
+    stats = srv.run(reqs)
+    assert stats["completed"] == 2 and stats["failed"] == 1
+    assert "diverged" in reqs[1].rejected
+    assert 1 not in srv.batch.solves
 
 
 def test_time_limit_reports_the_backlog():
