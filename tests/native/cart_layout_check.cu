@@ -63,7 +63,8 @@ void check_np() {
 
 int main() {
   check_np<2, 2>(); check_np<2, 3>(); check_np<2, 4>(); check_np<2, 5>();
-  check_np<2, 6>(); check_np<2, 7>(); check_np<2, 8>();
+  check_np<2, 6>(); check_np<2, 7>(); check_np<2, 8>(); check_np<2, 9>(); check_np<2, 10>();
+  check_np<2, 11>(); check_np<2, 12>(); check_np<2, 13>();
   check_np<3, 2>(); check_np<3, 3>(); check_np<3, 4>(); check_np<3, 5>();
   check_np<3, 6>(); check_np<3, 7>(); check_np<3, 8>();
   if (failures) return 1;
