@@ -16,12 +16,13 @@ metric: DoF-updates/s = n_dofs x 5 stages / s (whole job, all ranks).
    memory: host->device copy, step, device->host copy, every step.
  - roofline: achieved HBM bandwidth of the stage kernel = algorithmic bytes
    per step (112 B/DoF mixed, 144 B/DoF FP64) / device time per step.
- - cpu_baseline: the CPU restatement (oracle, OpenMP, all host threads) on a
-   bounded sample (16^3 cells, same degree).
+ - cpu_baseline: the CPU restatement for axis-aligned cells (line form, FP64,
+   OpenMP, all host threads) on the same 64^3 workload, whole steps for about
+   8 s.
 
 --impl reference: the CPU implementation of the path on the host cores
 (the reference itself cannot be built: it needs deal.II, p4est and MPI), on
-the same metric; rank 0 only.
+the same metric and the same 64^3 workload; rank 0 only.
 Multi-GPU (torchrun): independent replicas, one solve per rank (the path
 does not shard), max time over ranks.
 """
@@ -207,21 +208,34 @@ def e2e_steps(op, dt, steps, warmup, torch):
     return ev0.elapsed_time(ev1), n * 8, n * 8
 
 
-def cpu_sample(degree, min_seconds=8.0):
-    """The CPU restatement (oracle) on a bounded sample of the workload."""
+def cpu_problem(cells, degree):
+    """The headline workload on the CPU: the oracle's mesh and initial field,
+    stepped by the CPU baseline for axis-aligned cells (oracle/ew_cpu_cart.cpp:
+    the same operator and LSRK45 step in line form, FP64, OpenMP over all
+    host threads)."""
     import numpy as np
     from oracle import oracle
     oracle.build()
-    cells = 16
     prob = oracle.Problem.hypercube(3, degree, cells, 0, 0.0, 2)
+    n = prob.n_cells
+    cpu = oracle.CartCPU(3, degree, prob.vertices(), prob.neighbors(), np.ones(n), np.ones(n))
     dt = prob.time_step(0.25 / degree ** 1.5)
     u = prob.project_modes(*MODES)
+    return oracle, prob, cpu, dt, u
+
+
+def cpu_sample(degree, cells=64, min_seconds=8.0):
+    """The CPU baseline on the headline workload itself (64^3 cells), timed
+    over whole steps until at least min_seconds have passed."""
+    import numpy as np
+    oracle, prob, cpu, dt, u = cpu_problem(cells, degree)
     v = np.zeros_like(u)
-    prob.lsrk45_step(dt, u, v)  # warm-up
+    cpu.lsrk45_step(dt, u, v)  # warm-up (first touch of the pages)
+    u, v = v, u
     steps = 0
     t0 = time.perf_counter()
     while True:
-        prob.lsrk45_step(dt, v, u)
+        cpu.lsrk45_step(dt, u, v)
         u, v = v, u
         steps += 1
         el = time.perf_counter() - t0
@@ -229,8 +243,9 @@ def cpu_sample(degree, min_seconds=8.0):
             break
     rate = prob.n_dofs * STAGES * steps / el
     return {"value": rate, "unit": "DoF-updates/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": "3-D k=%d, %d^3 affine cells (%d DoFs), %d LSRK45 steps, OpenMP"
-                      % (degree, cells, prob.n_dofs, steps)}
+            "sample": "3-D k=%d, %d^3 affine cells (%d DoFs, the headline workload), %d LSRK45 "
+                      "steps of the CPU restatement for axis-aligned cells (line form, FP64, "
+                      "OpenMP)" % (degree, cells, prob.n_dofs, steps)}
 
 
 def traffic_from_profiles(precision, n_dofs):
@@ -252,32 +267,29 @@ def run_reference(args):
     if rank != 0:
         return
     import numpy as np
-    from oracle import oracle
-    oracle.build()
-    cells = 16
-    prob = oracle.Problem.hypercube(3, args.degree, cells, 0, 0.0, 2)
-    dt = prob.time_step(0.25 / args.degree ** 1.5)
-    u = prob.project_modes(*MODES)
+    oracle, prob, cpu, dt, u = cpu_problem(args.cells, args.degree)
     v = np.zeros_like(u)
     for _ in range(args.warmup):
-        prob.lsrk45_step(dt, u, v)
+        cpu.lsrk45_step(dt, u, v)
         u, v = v, u
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        prob.lsrk45_step(dt, u, v)
+        cpu.lsrk45_step(dt, u, v)
         u, v = v, u
     el = time.perf_counter() - t0
     value = prob.n_dofs * STAGES * args.steps / el
-    sample = ("3-D k=%d, %d^3 affine cells (%d DoFs) per step; the reference (deal.II "
-              "MatrixFree) cannot be built on this image, the CPU restatement of its arithmetic "
-              "is timed" % (args.degree, cells, prob.n_dofs))
+    sample = ("3-D k=%d, %d^3 affine cells (%d DoFs), %d timed steps after %d warm-up steps; "
+              "the reference (deal.II MatrixFree) cannot be built on this image: its arithmetic "
+              "restated for axis-aligned cells in line form (FP64, OpenMP over all host threads) "
+              "is timed" % (args.degree, args.cells, prob.n_dofs, args.steps, args.warmup))
     line = {
         "impl": "reference", "metric": "DoF-updates/s", "value": value, "unit": "DoF-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "3-D membrane, FE_DGQ(%d) hexes, LSRK45 (sampled at %d^3 cells)"
-                               % (args.degree, cells), "precision": "fp64"},
+        "config": {"workload": "3-D vibrating membrane, %d^3 affine hexes, FE_DGQ(%d), LSRK45"
+                               % (args.cells, args.degree), "precision": "fp64",
+                   "n_dofs": prob.n_dofs},
         "cpu_baseline": {"value": value, "unit": "DoF-updates/s", "cores": oracle.num_threads(),
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "DoF-updates/s", "h2d_bytes_per_step": 0,

@@ -252,5 +252,71 @@ class Problem:
         return rows[:nr].copy(), float(dt[0])
 
 
+def gauss_data(np_):
+    """1-D Gauss-Legendre data on [0, 1]: points, weights, the derivative
+    matrix D[i, j] = l_j'(x_i) of the Lagrange basis on the points, and the
+    traces l_j(0), l_j(1)."""
+    x, w = np.polynomial.legendre.leggauss(np_)
+    x, w = 0.5 * (x + 1.0), 0.5 * w
+    D = np.zeros((np_, np_))
+    L0, L1 = np.ones(np_), np.ones(np_)
+    for j in range(np_):
+        others = [m for m in range(np_) if m != j]
+        den = np.prod([x[j] - x[m] for m in others])
+        L0[j] = np.prod([0.0 - x[m] for m in others]) / den
+        L1[j] = np.prod([1.0 - x[m] for m in others]) / den
+        for i in range(np_):
+            s = 0.0
+            for a in others:
+                s += np.prod([x[i] - x[m] for m in others if m != a])
+            D[i, j] = s / den
+    return x, w, D, L0, L1
+
+
+class CartCPU:
+    """CPU baseline for axis-aligned meshes (``ew_cpu_cart.cpp``): the same
+    operator and LSRK45 step as the oracle in the line form, OpenMP over
+    cells; timed by ``bench.py``'s CPU legs and checked against ``Problem``
+    by the tests."""
+
+    def __init__(self, dim, degree, vertices, neighbors, speed, density):
+        L = lib()
+        P = ctypes.c_void_p
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.ewc_create.restype = P
+        L.ewc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, dp,
+                                 ctypes.POINTER(ctypes.c_int32), dp, dp, dp, dp, dp, dp]
+        L.ewc_destroy.argtypes = [P]
+        L.ewc_apply.argtypes = [P, dp, dp]
+        L.ewc_lsrk45_step.argtypes = [P, ctypes.c_double, dp, dp, dp]
+        np_ = degree + 1
+        _, w, D, L0, L1 = gauss_data(np_)
+        self.keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (vertices, speed, density)]
+        self.keep.append(np.ascontiguousarray(neighbors, dtype=np.int32))
+        self.keep += [np.ascontiguousarray(a, dtype=np.float64) for a in (w, D, L0, L1)]
+        v, sp, de, nb, w_, D_, L0_, L1_ = self.keep
+        self.n_cells = sp.shape[0]
+        self.n_dofs = self.n_cells * (dim + 1) * np_ ** dim
+        self.h = L.ewc_create(dim, np_, self.n_cells, _dp(v),
+                              nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dp(sp), _dp(de),
+                              _dp(w_), _dp(D_), _dp(L0_), _dp(L1_))
+        if not self.h:
+            raise RuntimeError("CartCPU: not an axis-aligned mesh or unsupported degree")
+        self.tmp = np.zeros(self.n_dofs)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ewc_destroy(self.h)
+            self.h = None
+
+    def apply(self, src):
+        dst = np.zeros_like(src)
+        lib().ewc_apply(self.h, _dp(src), _dp(dst))
+        return dst
+
+    def lsrk45_step(self, dt, vec_n, vec_np):
+        lib().ewc_lsrk45_step(self.h, dt, _dp(vec_n), _dp(vec_np), _dp(self.tmp))
+
+
 def num_threads():
     return lib().ewo_num_threads()
