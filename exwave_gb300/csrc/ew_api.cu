@@ -549,6 +549,7 @@ struct ew_ctx {
   // axis-aligned cells served by the line kernel (it is built for every
   // degree in 2-D and up to degree 7 in 3-D; otherwise the generic kernel)
   bool line = false;
+  bool spectral = true;  // ADER: spectral evaluation with degree reduction
   int cb_stage = 1, cb_ck = 1;
   const ew::KernelTable* kt = nullptr;
   int32_t* d_nbr = nullptr;
@@ -826,6 +827,13 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
   return EW_OK;
 }
 
+// The CK kernel of the context: precision, cell kind, post-processing and
+// spectral evaluation (below degree 4 both evaluations are the same kernel).
+const ew::KernelEntry& ck_entry(const ew_ctx* c) {
+  const int p = c->ff ? 2 : (c->mixed ? 1 : 0), ca = c->cart ? 1 : 0, po = c->post ? 1 : 0;
+  return (c->spectral || c->np < 5) ? c->kt->ck[p][ca][po] : c->kt->ck_full[p][ca][po];
+}
+
 int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
   ew::LaunchArgs a = base_args(c, true);
   a.single.X = src;
@@ -845,7 +853,7 @@ int launch_ck(ew_ctx* c, double dt, const double* src, void* T) {
     a.ck_fac[s] = (float)(fac * dtp);
     dtp *= dt;
   }
-  const ew::KernelEntry& k = c->kt->ck[c->ff ? 2 : (c->mixed ? 1 : 0)][c->cart ? 1 : 0][c->post ? 1 : 0];
+  const ew::KernelEntry& k = ck_entry(c);
   if (!k.launch)
     return fail(c, EW_ERR_UNSUPPORTED,
                 "ADER: the Cauchy-Kovalevskaya kernel is built for 3-D degrees up to 7 (all degrees in 2-D)");
@@ -956,10 +964,6 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
       opt.precision != EW_PREC_MIXED_FF)
     return fail(nullptr, EW_ERR_INVALID,
                 "precision must be EW_PREC_FP64, EW_PREC_MIXED or EW_PREC_MIXED_FF");
-  if (!opt.spectral_evaluation)
-    return fail(nullptr, EW_ERR_UNSUPPORTED,
-                "ADER with spectral_evaluation = false is not built (only the spectral "
-                "Cauchy-Kovalevskaya procedure)");
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev == 0)
@@ -986,6 +990,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   c->ff = opt.precision == EW_PREC_MIXED_FF;
   c->cart = cart;
   c->post = opt.use_ader_post != 0;
+  c->spectral = opt.spectral_evaluation != 0;
   c->kt = &ew::kernel_table(c->dim, c->np);
   c->line = cart && c->kt->cart[ew::CV_F64_MID].launch != nullptr;
   const int dim = c->dim, nv = 1 << dim;
@@ -1132,8 +1137,7 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
   c->cb_stage = default_cb(c->N, opt.cells_per_block);
   // mixed CK kernel: 80 registers a thread, two blocks per SM need 384 threads or fewer
   c->cb_ck = c->mixed && !c->ff ? std::max(1, std::min(c->cb_stage, 384 / c->N)) : c->cb_stage;
-  const int ck_var = c->ff ? 2 : (c->mixed ? 1 : 0);
-  const ew::KernelEntry& ckk = c->kt->ck[ck_var][cart][c->post];
+  const ew::KernelEntry& ckk = ck_entry(c);
   while (ckk.smem && c->cb_ck > 1 && ckk.smem(c->cb_ck) > 200 * 1024) --c->cb_ck;
   if (c->line) {
     const int lines = c->kt->lines;

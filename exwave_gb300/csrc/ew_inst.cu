@@ -92,15 +92,15 @@ struct StageK {
   }
 };
 
-template <typename Real, typename InT, typename OutT, bool CART, bool POST>
+template <typename Real, typename InT, typename OutT, bool CART, bool POST, bool SPEC = true>
 struct CkK {
   static size_t smem(int cb) { return (size_t)CkSmem<DIM, NP, CART>(cb).end * sizeof(Real); }
   static cudaError_t launch(const LaunchArgs& a, int grid, cudaStream_t st) {
     const int cb = a.cells_per_block;
-    return run(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST>, a, grid, cb * N, smem(cb), st);
+    return run(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST, SPEC>, a, grid, cb * N, smem(cb), st);
   }
   static int occupancy(int cb) {
-    return blocks_per_sm(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST>, cb * N, smem(cb));
+    return blocks_per_sm(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST, SPEC>, cb * N, smem(cb));
   }
 };
 
@@ -195,18 +195,17 @@ void EW_TABLE_FN(KernelTable& t) {
     fill_cart<CartK<FF, FF, EPI_APPLY>>(t.cart[CV_FF_APPLYFF]);
     fill_cart<CartK<FF, FF, EPI_FF_LAST_PAIR>>(t.cart[CV_FF_LAST_PAIR]);
   }
-  // stage kernels: [variant][cart]
+  // stage kernels: [variant][cart]; curved cells, and axis-aligned cells
+  // where the line kernel is not built
   fill<StageK<double, double, double, false>>(t.stage[STAGE_F64][0]);
-  fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);
   fill<StageK<float, double, float, false>>(t.stage[STAGE_MIX_IN64][0]);
-  fill<StageK<float, double, float, true>>(t.stage[STAGE_MIX_IN64][1]);
   fill<StageK<float, float, float, false>>(t.stage[STAGE_MIX_IN32][0]);
-  fill<StageK<float, float, float, true>>(t.stage[STAGE_MIX_IN32][1]);
-  // compensated: curved cells (axis-aligned cells use the line kernel where it is built)
   fill<StageK<FF, double, FF, false>>(t.stage[STAGE_FF_IN64][0]);
   fill<StageK<FF, FF, FF, false>>(t.stage[STAGE_FF_INFF][0]);
   if constexpr (!LINE_OK) {
-    // axis-aligned cells without the line kernel
+    fill<StageK<double, double, double, true>>(t.stage[STAGE_F64][1]);
+    fill<StageK<float, double, float, true>>(t.stage[STAGE_MIX_IN64][1]);
+    fill<StageK<float, float, float, true>>(t.stage[STAGE_MIX_IN32][1]);
     fill<StageK<FF, double, FF, true>>(t.stage[STAGE_FF_IN64][1]);
     fill<StageK<FF, FF, FF, true>>(t.stage[STAGE_FF_INFF][1]);
   }
@@ -224,6 +223,22 @@ void EW_TABLE_FN(KernelTable& t) {
     fill<CkK<FF, double, FF, false, true>>(t.ck[2][0][1]);
     fill<CkK<FF, double, FF, true, false>>(t.ck[2][1][0]);
     fill<CkK<FF, double, FF, true, true>>(t.ck[2][1][1]);
+    // without spectral evaluation (no degree reduction; from k = 4 on the
+    // two differ)
+    if constexpr (NP >= 5) {
+      fill<CkK<double, double, double, false, false, false>>(t.ck_full[0][0][0]);
+      fill<CkK<double, double, double, false, true, false>>(t.ck_full[0][0][1]);
+      fill<CkK<double, double, double, true, false, false>>(t.ck_full[0][1][0]);
+      fill<CkK<double, double, double, true, true, false>>(t.ck_full[0][1][1]);
+      fill<CkK<float, double, float, false, false, false>>(t.ck_full[1][0][0]);
+      fill<CkK<float, double, float, false, true, false>>(t.ck_full[1][0][1]);
+      fill<CkK<float, double, float, true, false, false>>(t.ck_full[1][1][0]);
+      fill<CkK<float, double, float, true, true, false>>(t.ck_full[1][1][1]);
+      fill<CkK<FF, double, FF, false, false, false>>(t.ck_full[2][0][0]);
+      fill<CkK<FF, double, FF, false, true, false>>(t.ck_full[2][0][1]);
+      fill<CkK<FF, double, FF, true, false, false>>(t.ck_full[2][1][0]);
+      fill<CkK<FF, double, FF, true, true, false>>(t.ck_full[2][1][1]);
+    }
   }
 }
 

@@ -628,10 +628,14 @@ struct CkState {
 // derivative j = s + 2 at level r = s/2 (M = NP - 2r points per direction),
 // added to the level's contribution; after odd steps the field set is
 // L2-projected onto the next lower level (degree - 2).
-template <int DIM, int NP, typename Real, bool CART, int S, int NSTEPS, typename Acc>
+// Without spectral evaluation (SPEC false) every step stays on level 0: in the
+// Gauss collocation basis the reference's submit / integrate / inverse mass
+// of each derivative (wave_equation_operations.cc:1205-1233) is the identity,
+// so only the degree reduction goes away.
+template <int DIM, int NP, typename Real, bool CART, int S, int NSTEPS, typename Acc, bool SPEC>
 __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Acc* c0) {
   constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
-  constexpr int R = S / 2;
+  constexpr int R = SPEC ? S / 2 : 0;
   constexpr int M = NP - 2 * R;
   constexpr int NM = ipow_c(M, DIM);
   constexpr int GEO = CART ? DIM : (1 << DIM) * DIM;
@@ -656,11 +660,11 @@ __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Acc
   }
   __syncthreads();
   if constexpr (S + 1 < NSTEPS) {
-    if constexpr (S % 2 == 1) {
+    if constexpr (SPEC && S % 2 == 1) {
       const Level<Real> Ln = get_level(st.sB, NP, R + 1);
       tensor_ct<DIM, Real, M - 2, M>(Ln.P, st.sS, F * N, st.sS, F * N, st.sT1, st.sT2, F * N, st.nc, F);
     }
-    ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS, Acc>(st, fac, c0);
+    ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS, Acc, SPEC>(st, fac, c0);
   }
 }
 
@@ -692,14 +696,15 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Acc* c0) {
   }
 }
 
-template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST>
+template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST,
+          bool SPEC = true>
 __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const LaunchArgs La) {
   using S = Shape<DIM, NP, CART>;
   constexpr int F = S::F, N = S::N;
   constexpr int NL = n_levels(NP);
   // Taylor terms j = 0..max(k,2); derivatives j >= 2 come from the steps
   constexpr int NSTEPS = (NP - 2 > 1) ? NP - 2 : 1;
-  constexpr int RLAST = (NSTEPS - 1) / 2;
+  constexpr int RLAST = SPEC ? (NSTEPS - 1) / 2 : 0;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real* sm = reinterpret_cast<Real*>(smem_raw);
   const int CB = La.cells_per_block;
@@ -840,7 +845,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     st.active = active;
     st.rho = rho;
     st.c_sq = c_sq;
-    ck_steps<DIM, NP, Real, CART, 0, NSTEPS, Acc>(st, fac, c0);
+    ck_steps<DIM, NP, Real, CART, 0, NSTEPS, Acc, SPEC>(st, fac, c0);
     ck_gather<DIM, NP, Real, RLAST, Acc>(st, c0);
     if (active) {
       OutT* T = static_cast<OutT*>(sd.Xout);

@@ -61,6 +61,9 @@ struct KernelTable {
   KernelEntry stage[N_STAGE_VARIANTS][2];  // [variant][cartesian]
   CartEntry cart[N_CART_VARIANTS];
   KernelEntry ck[3][2][2];                 // [FP64 / mixed / compensated][cartesian][post]
+  // the same without spectral evaluation (no degree reduction); empty below
+  // degree 4, where both are the same
+  KernelEntry ck_full[3][2][2];
   // upload the even-odd 1D constants of this degree to the current device
   cudaError_t (*set_constants)(const double* w, const double* D, const double* L0,
                                const double* L1) = nullptr;

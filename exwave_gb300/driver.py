@@ -37,7 +37,8 @@ def run(params, precision="fp64", on_output=None, output_dir="output"):
     m = mesh_mod.hypercube(dim, params["n_initial_intervals"], params["n_refinements"],
                            params["grid_transform_factor"], "reference", params["boundary_id"])
     op = WaveEquationOperation(m, k, precision=precision,
-                               use_ader_post=params["use_ader_post"] and integ == "ADER")
+                               use_ader_post=params["use_ader_post"] and integ == "ADER",
+                               spectral_evaluation=params.get("spectral_evaluation", True))
     amps, kv = reference_mode(dim, params["membrane_modes"])
     tc = TimeControl()
     dt0 = mesh_mod.time_step_size(m, params["cfl_scaled"])

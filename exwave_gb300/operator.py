@@ -38,7 +38,7 @@ class WaveEquationOperation:
     integrator, ADER included)."""
 
     def __init__(self, mesh, degree, precision="fp64", use_ader_post=False, cells_per_block=0,
-                 device=0):
+                 device=0, spectral_evaluation=True):
         import torch
         self.torch = torch
         self.L = _lib.load()
@@ -63,7 +63,7 @@ class WaveEquationOperation:
         op = _lib.Options()
         op.precision = PRECISIONS[precision]
         op.use_ader_post = int(self.use_ader_post)
-        op.spectral_evaluation = 1
+        op.spectral_evaluation = int(bool(spectral_evaluation))
         op.cells_per_block = cells_per_block
         op.device = device
         h = ctypes.c_void_p()

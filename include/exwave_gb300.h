@@ -84,7 +84,8 @@ typedef struct ew_mesh_desc {
 typedef struct ew_options {
   int32_t precision;           /* ew_precision */
   int32_t use_ader_post;       /* reference parameter ADER/use_ader_post */
-  int32_t spectral_evaluation; /* reference ADER/spectral_evaluation; only 1 */
+  int32_t spectral_evaluation; /* reference ADER/spectral_evaluation (parameters.cc:76):
+                                  1 (default) degree reduction, 0 full degree throughout */
   int32_t cells_per_block;     /* 0: tuned default */
   int32_t device;              /* CUDA device ordinal */
 } ew_options;

@@ -319,6 +319,7 @@ struct Oracle {
   std::vector<char> cartesian;   // per cell: axis-aligned box
   std::vector<double> h;         // per cell extents (cartesian cells)
   int use_ader_post = 0;
+  int spectral = 1;  // ADER: spectral evaluation with degree reduction (parameters.cc:76)
   // lower-degree collocation data for the ADER degree reduction
   std::vector<Basis1D> levels;     // levels[r]: n - 2r Gauss points
   std::vector<std::vector<double>> proj;    // proj[r]: (n_r-2) x n_r
@@ -625,6 +626,11 @@ struct Oracle {
   // Cauchy-Kovalevskaya procedure with spectral evaluation and degree
   // reduction every second derivative (integrate_taylor_cauchykovalewski,
   // wave_equation_operations.cc:961-1059, and its recursive step 1063-1262).
+  // Without spectral evaluation (:1013, 1037, 1086-1090, 1205-1233) every
+  // derivative is submitted, integrated, multiplied by the inverse mass
+  // matrix and its gradient evaluated at the full degree: in the Gauss
+  // collocation basis the first three are the identity, so the recursion runs
+  // on level 0 throughout and no degree is reduced.
   // `d1` holds the values of the first time derivative when use_ader_post
   // is set (the full DG operator applied to src), else null.
   void ck_cell(int64_t c, const double* src, const double* d1, double dt, double* T) const {
@@ -653,7 +659,7 @@ struct Oracle {
     int r = 0;
     std::vector<double> Snew, Sproj;
     for (int s = 0; s < n_steps; ++s) {
-      r = s / 2;
+      r = spectral ? s / 2 : 0;
       if (contrib[r].empty()) contrib[r].assign(F * ipow(levels[r].n, dim), 0.0);
       ck_derivative(c, r, S, Snew, rho, c_sq);
       double fac = -0.5;
@@ -661,7 +667,7 @@ struct Oracle {
       const double fac_t = fac * std::pow(dt, s + 3);
       for (size_t i = 0; i < Snew.size(); ++i) contrib[r][i] += fac_t * Snew[i];
       S.swap(Snew);
-      if (s + 1 < n_steps && (s % 2) == 1) {
+      if (spectral && s + 1 < n_steps && (s % 2) == 1) {
         tensor_apply(proj[r], levels[r + 1].n, levels[r].n, S, Sproj);
         S.swap(Sproj);
       }
@@ -1010,6 +1016,7 @@ int64_t ewo_n_dofs(ewo_problem* p) { return (int64_t) reinterpret_cast<Oracle*>(
 const double* ewo_vertices(ewo_problem* p) { return reinterpret_cast<Oracle*>(p)->mesh.vert.data(); }
 const int32_t* ewo_neighbors(ewo_problem* p) { return reinterpret_cast<Oracle*>(p)->mesh.nbr.data(); }
 void ewo_set_ader_post(ewo_problem* p, int on) { reinterpret_cast<Oracle*>(p)->use_ader_post = on; }
+void ewo_set_spectral(ewo_problem* p, int on) { reinterpret_cast<Oracle*>(p)->spectral = on; }
 
 // dt = cfl * min_cells(min vertex distance / c) (explicit_wave.cc:529-545);
 // cfl is the already-scaled Courant number (parameters.cc:195).

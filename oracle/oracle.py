@@ -59,6 +59,7 @@ def lib():
         L.ewo_neighbors.restype = i32p
         L.ewo_neighbors.argtypes = [P]
         L.ewo_set_ader_post.argtypes = [P, ctypes.c_int]
+        L.ewo_set_spectral.argtypes = [P, ctypes.c_int]
         L.ewo_time_step.restype = ctypes.c_double
         L.ewo_time_step.argtypes = [P, ctypes.c_double]
         L.ewo_quadrature_points.argtypes = [P, dp]
@@ -142,6 +143,10 @@ class Problem:
 
     def set_ader_post(self, on):
         lib().ewo_set_ader_post(self.h, int(bool(on)))
+
+    def set_spectral(self, on):
+        """ADER with (the default) or without spectral evaluation."""
+        lib().ewo_set_spectral(self.h, int(bool(on)))
 
     def time_step(self, cfl_scaled):
         return lib().ewo_time_step(self.h, cfl_scaled)

@@ -331,3 +331,33 @@ def test_compensated_rejects_static_step(env):
     a, b = op.new_vector(), op.new_vector()
     from exwave_gb300.operator import _ptr
     assert op.L.ew_lsrk45_step_static(op.ctx, 0.01, _ptr(a), _ptr(b)) == -2  # EW_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("case", [CASES[i] for i in (1, 5, 10, 12, 13)], ids=ids)
+@pytest.mark.parametrize("post", [False, True])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_ff", "mixed"])
+def test_ader_step_without_spectral_evaluation(env, case, post, precision):
+    """ADER with spectral_evaluation = false (the CK recursion at full degree
+    throughout) against the oracle: two steps, the tolerances of test_ader_step."""
+    ew, oracle, torch = env
+    dim, k, n, ref, f, bids, het = case
+    m = make_case(ew, dim, n, ref, f, bids, het, seed=12)
+    op = ew.WaveEquationOperation(m, k, precision=precision, use_ader_post=post,
+                                  spectral_evaluation=False)
+    o = oracle.Problem.from_mesh(dim, k, m.vertices, m.neighbors, m.speed, m.density)
+    o.set_ader_post(post)
+    o.set_spectral(False)
+    u0 = o.project_reference(2)
+    dt = o.time_step(0.2 / k ** 1.5)
+    a, b = u0.copy(), np.zeros_like(u0)
+    vn = torch.from_numpy(u0.copy()).cuda()
+    vnp = torch.zeros_like(vn)
+    for _ in range(2):
+        o.ader_step(dt, a, b)
+        a, b = b, a
+        op.ader_step(dt, vn, vnp)
+        vn, vnp = vnp, vn
+    op.synchronize()
+    tol = {"fp64": FP64_TOL, "mixed_ff": FF_TOL, "mixed": MIXED_ADER_STEP_TOL}[precision]
+    err = np.abs(vn.cpu().numpy() - a).max() / np.abs(a).max()
+    assert err < tol, err
