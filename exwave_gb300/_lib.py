@@ -27,7 +27,8 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_batch_bytes_free", "ew_batch_add", "ew_batch_remove", "ew_batch_set_state",
            "ew_batch_get_state", "ew_batch_step", "ew_batch_info", "ew_batch_diverged", "ew_batch_receivers",
            "ew_batch_set_stream", "ew_batch_synchronize", "ew_batch_kernel_launches",
-           "ew_tune_set", "ew_tune_get", "ew_lsrk45_step_static", "ew_lsrk45_steps",
+           "ew_tune_set", "ew_tune_get", "ew_tune_set_staging", "ew_tune_get_staging",
+           "ew_lsrk45_step_static", "ew_lsrk45_steps",
            "ew_set_receivers", "ew_sample_receivers", "ew_aderadconfull_step",
            "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update", "ew_check_wait_timeout"]
 
@@ -49,7 +50,7 @@ class MeshDesc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("use_ader_post", ctypes.c_int32),
                 ("spectral_evaluation", ctypes.c_int32), ("cells_per_block", ctypes.c_int32),
-                ("device", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("nb_staging", ctypes.c_int32)]
 
 
 class HypercubeDesc(ctypes.Structure):
@@ -107,6 +108,8 @@ def load():
         "ew_kernel_launches": (i64, [vp]),
         "ew_tune_set": (ctypes.c_int, [i32, i32, i32, i32]),
         "ew_tune_get": (i32, [i32, i32, i32]),
+        "ew_tune_set_staging": (ctypes.c_int, [i32, i32, i32, i32]),
+        "ew_tune_get_staging": (i32, [i32, i32, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -129,8 +132,9 @@ def _apply_tuning(L):
     except (OSError, ValueError):
         return
     for e in table.get("entries", []):
-        L.ew_tune_set(int(e["dim"]), int(e["degree"]), 1 if e["precision"] == "mixed" else 0,
-                      int(e["cells_per_block"]))
+        prec = {"fp64": 0, "mixed": 1, "mixed_ff": 2}[e["precision"]]
+        L.ew_tune_set(int(e["dim"]), int(e["degree"]), prec, int(e["cells_per_block"]))
+        L.ew_tune_set_staging(int(e["dim"]), int(e["degree"]), prec, int(e.get("nb_staging", 0)))
 
 
 def check(rc, ctx=None):

@@ -1,11 +1,17 @@
-"""Autotuner of the operator kernel's cells per thread block.
+"""Autotuner of the line kernel's launch shape and shared-memory layout.
 
-For every (dimension, degree, precision) it builds a Cartesian membrane
-problem of about `target_dofs` DoFs, times LSRK45 steps with each admissible
-cells-per-block value (threads per block = cells x lines of the Cartesian
-kernel, at most 512) and keeps the fastest.  The table is written to
+For every (dimension, degree, precision: FP64, FP32 operator, compensated)
+it builds a Cartesian membrane problem of about `target_dofs` DoFs and times
+LSRK45 steps over two knobs: the cells per thread block (threads per block =
+cells x lines of the kernel, one thread per (cell, direction, line), at most
+512) and, in 3-D where both are built, the shared-memory layout of the
+neighbour data (per-thread copies of each thread's neighbour lines, or bulk
+copies of the neighbours' whole field arrays).  It keeps the fastest pair.
+The threads per cell are fixed by the kernel's design (one per line), so
+they are not a knob.  The table is written to
 exwave_gb300/tuning/tuning.json and loaded by the library at import
-(``ew_tune_set``), where ew_create and the batch runtime use it.
+(``ew_tune_set``, ``ew_tune_set_staging``), where ew_create and the batch
+runtime use it.
 
 Usage on the GPU: python -m exwave_gb300.autotune [--target-dofs 4e7]
 """
@@ -33,10 +39,18 @@ def candidates(dim, degree):
     return c
 
 
-def time_case(dim, degree, precision, cells, cb, steps, torch):
+def stagings(dim, degree, precision):
+    """Neighbour layouts built for this case: 1 per-thread lines, 2 bulk arrays."""
+    np_ = degree + 1
+    bulk = dim == 3 and (np_ >= 6 or (np_ == 4 and precision == "mixed"))
+    return [1, 2] if bulk else [1]
+
+
+def time_case(dim, degree, precision, cells, cb, steps, torch, staging=0):
     m = mesh_mod.hypercube(dim, cells)
     dt = mesh_mod.time_step_size(m, 0.25 / degree ** 1.5)
-    op = WaveEquationOperation(m, degree, precision=precision, cells_per_block=cb)
+    op = WaveEquationOperation(m, degree, precision=precision, cells_per_block=cb,
+                               nb_staging=staging)
     u = op.project_membrane([1.0], [[1] * dim])
     v = torch.zeros_like(u)
     stream = torch.cuda.current_stream()
@@ -55,8 +69,8 @@ def time_case(dim, degree, precision, cells, cb, steps, torch):
     return n * 5 * steps / (ms / 1e3)
 
 
-def run(dims=(2, 3), degrees=range(1, 8), precisions=("mixed", "fp64"), target_dofs=4e7, steps=4,
-        log=print):
+def run(dims=(2, 3), degrees=range(1, 8), precisions=("mixed", "mixed_ff", "fp64"), target_dofs=4e7,
+        steps=4, log=print):
     import torch
     entries = []
     for dim in dims:
@@ -66,17 +80,19 @@ def run(dims=(2, 3), degrees=range(1, 8), precisions=("mixed", "fp64"), target_d
             for prec in precisions:
                 best = None
                 res = {}
-                for cb in candidates(dim, k):
-                    rate = time_case(dim, k, prec, cells, cb, steps if prec == "mixed" else 2, torch)
-                    res[cb] = rate
-                    if best is None or rate > res[best]:
-                        best = cb
+                for st in stagings(dim, k, prec):
+                    for cb in candidates(dim, k):
+                        rate = time_case(dim, k, prec, cells, cb, steps if prec == "mixed" else 2,
+                                         torch, staging=st)
+                        res[(cb, st)] = rate
+                        if best is None or rate > res[best]:
+                            best = (cb, st)
                 entries.append({"dim": dim, "degree": k, "precision": prec,
-                                "cells_per_block": best, "cells": cells,
-                                "rates": {str(c): r for c, r in res.items()}})
+                                "cells_per_block": best[0], "nb_staging": best[1], "cells": cells,
+                                "rates": {"%d/%d" % c: r for c, r in res.items()}})
                 if log:
-                    log("dim %d k %d %s: best cb %d (%.3g DoF-updates/s)" % (dim, k, prec, best,
-                                                                          res[best]))
+                    log("dim %d k %d %s: best cb %d staging %d (%.3g DoF-updates/s)"
+                        % (dim, k, prec, best[0], best[1], res[best]))
     return entries
 
 
@@ -90,7 +106,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--target-dofs", type=float, default=4e7)
     ap.add_argument("--dims", default="2,3")
-    ap.add_argument("--precisions", default="mixed,fp64")
+    ap.add_argument("--precisions", default="mixed,mixed_ff,fp64")
     args = ap.parse_args()
     import torch
     _lib.load()

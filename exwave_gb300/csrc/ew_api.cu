@@ -41,15 +41,25 @@ const KernelTable& kernel_table(int dim, int np) {
 }
 
 namespace {
-int g_tuned[2][EW_MAX_DEGREE + 1][2] = {};
+// per (dim, degree, precision: FP64 / mixed / compensated): cells per block
+// and neighbour staging of the line kernel
+int g_tuned[2][EW_MAX_DEGREE + 1][3] = {};
+int g_tuned_staging[2][EW_MAX_DEGREE + 1][3] = {};
 std::mutex g_tuned_mutex;
 }  // namespace
 
 int tuned_cells_per_block(int dim, int degree, int precision) {
-  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 || precision > 1)
+  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 || precision > 2)
     return 0;
   std::lock_guard<std::mutex> lk(g_tuned_mutex);
   return g_tuned[dim - 2][degree][precision];
+}
+
+int tuned_staging(int dim, int degree, int precision) {
+  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 || precision > 2)
+    return 0;
+  std::lock_guard<std::mutex> lk(g_tuned_mutex);
+  return g_tuned_staging[dim - 2][degree][precision];
 }
 
 cudaError_t upload_cart_constants(int dim, int np) {
@@ -549,6 +559,7 @@ struct ew_ctx {
   // axis-aligned cells served by the line kernel (it is built for every
   // degree in 2-D and up to degree 7 in 3-D; otherwise the generic kernel)
   bool line = false;
+  bool nb_lines = false;  // line kernel: per-thread neighbour lines even where bulk copies are built
   bool spectral = true;  // ADER: spectral evaluation with degree reduction
   int cb_stage = 1, cb_ck = 1;
   const ew::KernelTable* kt = nullptr;
@@ -816,7 +827,7 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
     const ew::CartEntry& k = c->kt->cart[cvar];
     const int occ = std::max(1, k.occupancy(c->cb_cart, sx));
     const int grid = std::max(1, std::min(c->n_work_cart, occ * c->num_sms));
-    e = k.launch(a, sx, tma ? 1 : 0, grid, c->stream);
+    e = k.launch(a, sx, tma ? 1 : 0, c->nb_lines ? 1 : 0, grid, c->stream);
   } else {
     const ew::KernelEntry& k = c->kt->stage[variant][c->cart ? 1 : 0];
     if (!k.launch) return fail(c, EW_ERR_UNSUPPORTED, "no stage kernel built for this mesh and precision");
@@ -1147,6 +1158,11 @@ int ew_create(const ew_mesh_desc* mesh, const ew_options* options, ew_ctx** out)
     c->cb_cart = std::max(1, std::min(c->cb_cart, std::max(1, 512 / lines)));
     const int v = c->ff ? ew::CV_FF_MID : (c->mixed ? ew::CV_MIX_MID : ew::CV_F64_MID);
     while (c->cb_cart > 1 && c->kt->cart[v].smem(c->cb_cart, 1) > 110 * 1024) --c->cb_cart;
+    if (opt.nb_staging < 0 || opt.nb_staging > 2)
+      return bail(fail(c, EW_ERR_INVALID, "nb_staging must be 0, 1 or 2"));
+    const int staging = opt.nb_staging > 0 ? opt.nb_staging
+                                           : ew::tuned_staging(c->dim, c->degree, opt.precision);
+    c->nb_lines = staging == 1;
   }
   if ((rc = build_work(c, c->cb_stage, &c->d_work_stage, &c->n_work_stage)) ||
       (rc = build_work(c, c->cb_ck, &c->d_work_ck, &c->n_work_ck)) ||
@@ -1720,7 +1736,7 @@ int ew_l2_difference(ew_ctx* ctx, const double* a, const double* b, double out[2
 
 int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_per_block) {
   if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 ||
-      precision > 1 || cells_per_block < 0 || cells_per_block > 1024)
+      precision > 2 || cells_per_block < 0 || cells_per_block > 1024)
     return EW_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ew::g_tuned_mutex);
   ew::g_tuned[dim - 2][degree][precision] = cells_per_block;
@@ -1729,6 +1745,19 @@ int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_pe
 
 int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision) {
   return ew::tuned_cells_per_block(dim, degree, precision);
+}
+
+int ew_tune_set_staging(int32_t dim, int32_t degree, int32_t precision, int32_t nb_staging) {
+  if (dim < 2 || dim > 3 || degree < 1 || degree > EW_MAX_DEGREE || precision < 0 ||
+      precision > 2 || nb_staging < 0 || nb_staging > 2)
+    return EW_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ew::g_tuned_mutex);
+  ew::g_tuned_staging[dim - 2][degree][precision] = nb_staging;
+  return EW_OK;
+}
+
+int32_t ew_tune_get_staging(int32_t dim, int32_t degree, int32_t precision) {
+  return ew::tuned_staging(dim, degree, precision);
 }
 
 int ew_set_receivers(ew_ctx* ctx, int32_t n, const double* points) {

@@ -195,6 +195,7 @@ struct Group {
   int grid[2][5] = {{0}};
   int sx[5] = {0}, variant[5] = {0};
   int tma = 0;
+  int nb_lines = 0;  // tuned neighbour staging of the line kernel
 };
 
 template <typename T>
@@ -429,7 +430,9 @@ int rebuild(ew_batch* b) {
     g.members = kv.second;
     const ew::KernelTable& kt = ew::kernel_table(g.dim, g.np);
     const int lines = kt.lines;
-    const int tuned = b->ff ? 0 : ew::tuned_cells_per_block(g.dim, g.np - 1, b->mixed ? 1 : 0);
+    const int prec = b->ff ? 2 : (b->mixed ? 1 : 0);
+    const int tuned = ew::tuned_cells_per_block(g.dim, g.np - 1, prec);
+    g.nb_lines = ew::tuned_staging(g.dim, g.np - 1, prec) == 1 ? 1 : 0;
     g.cb = tuned > 0 ? std::min(tuned, std::max(1, 512 / lines)) : std::max(1, 256 / lines);
     const int NP = g.np;
     int N = 1;
@@ -546,7 +549,7 @@ int launch_step(ew_batch* b, int p) {
       a.n_work = g.n_work;
       a.cells_per_block = g.cb;
       a.err = b->d_err;
-      e = kt.cart[g.variant[st]].launch(a, g.sx[st], g.tma, g.grid[p][st], b->stream);
+      e = kt.cart[g.variant[st]].launch(a, g.sx[st], g.tma, g.nb_lines, g.grid[p][st], b->stream);
       if (e != cudaSuccess) return bcuda(b, e, "batch stage launch");
       ++n;
     }

@@ -496,8 +496,10 @@ __device__ __forceinline__ void store2(FF* p, FF a, FF b) {
 
 struct CartArgs {
   LaunchArgs la;
-  int32_t stage_x;  // X staged in shared memory (else read from A's buffer: X == A)
-  int32_t tma;      // bulk copies usable (alignment checked on the host)
+  int32_t stage_x;   // X staged in shared memory (else read from A's buffer: X == A)
+  int32_t tma;       // bulk copies usable (alignment checked on the host)
+  int32_t nb_lines;  // neighbour lines by per-thread copies even where bulk copies are built
+  int32_t pad;
 };
 
 #ifndef EW_FF_MAXNREG
@@ -580,7 +582,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
   // cell's data is a multiple of 16 bytes, so that the rounded windows stay
   // inside the stage input array.
   constexpr int NB_SLOT = CartSmem<DIM, NP, Real, InT, A_ELEM>::NB_SLOT;
-  const bool nb_bulk = cart_nb_bulk<DIM, NP, InT>() && ca.tma != 0;
+  const bool nb_bulk = cart_nb_bulk<DIM, NP, InT>() && ca.tma != 0 && ca.nb_lines == 0;
   unsigned char* sNb = smem_cart + lay.nb;
   // byte offset of a neighbour's field array within its 16-byte window
   auto nb_rem = [](int nb, int f) -> int {

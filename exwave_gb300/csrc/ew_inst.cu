@@ -114,11 +114,13 @@ struct CartK {
   static size_t smem(int cb, int sx) {
     return CartSmem<DIM, NP, Real, InT, EpiTraits<EPI>::a_elem>(cb, sx != 0, SA).end;
   }
-  static cudaError_t launch(const LaunchArgs& a, int sx, int tma, int grid, cudaStream_t st) {
+  static cudaError_t launch(const LaunchArgs& a, int sx, int tma, int nb_lines, int grid,
+                            cudaStream_t st) {
     CartArgs ca;
     ca.la = a;
     ca.stage_x = sx;
     ca.tma = tma;
+    ca.nb_lines = nb_lines;
     const int cb = a.cells_per_block;
     const size_t sm = smem(cb, sx);
     auto kern = stage_cart_kernel<DIM, NP, Real, InT, EPI>;

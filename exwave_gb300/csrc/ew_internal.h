@@ -26,6 +26,8 @@ cudaError_t launch_wait_timeout(int polls, int* err, cudaStream_t stream);
 
 // Tuned cells per block for (dim, degree, precision); 0 when unset.
 int tuned_cells_per_block(int dim, int degree, int precision);
+// Tuned neighbour staging of the line kernel (0 unset, 1 lines, 2 bulk).
+int tuned_staging(int dim, int degree, int precision);
 
 // LowStorageRK45Reg2 coefficients (time_integrators.cc:243-252)
 constexpr double kA21 = 970286171893. / 4311952581923.;

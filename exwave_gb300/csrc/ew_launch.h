@@ -50,7 +50,8 @@ enum CartVariant : int {
 
 // Launcher of the Cartesian line kernel.
 struct CartEntry {
-  cudaError_t (*launch)(const LaunchArgs&, int stage_x, int tma, int grid, cudaStream_t) = nullptr;
+  cudaError_t (*launch)(const LaunchArgs&, int stage_x, int tma, int nb_lines, int grid,
+                        cudaStream_t) = nullptr;
   int (*occupancy)(int cells_per_block, int stage_x) = nullptr;
   size_t (*smem)(int cells_per_block, int stage_x) = nullptr;
 };

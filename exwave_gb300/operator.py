@@ -38,7 +38,7 @@ class WaveEquationOperation:
     integrator, ADER included)."""
 
     def __init__(self, mesh, degree, precision="fp64", use_ader_post=False, cells_per_block=0,
-                 device=0, spectral_evaluation=True):
+                 device=0, spectral_evaluation=True, nb_staging=0):
         import torch
         self.torch = torch
         self.L = _lib.load()
@@ -65,6 +65,7 @@ class WaveEquationOperation:
         op.use_ader_post = int(self.use_ader_post)
         op.spectral_evaluation = int(bool(spectral_evaluation))
         op.cells_per_block = cells_per_block
+        op.nb_staging = nb_staging
         op.device = device
         h = ctypes.c_void_p()
         _lib.check(self.L.ew_create(ctypes.byref(md), ctypes.byref(op), ctypes.byref(h)))

@@ -88,6 +88,11 @@ typedef struct ew_options {
                                   1 (default) degree reduction, 0 full degree throughout */
   int32_t cells_per_block;     /* 0: tuned default */
   int32_t device;              /* CUDA device ordinal */
+  /* shared-memory layout of the line kernel's neighbour data (3-D degrees
+   * where both are built): 0 tuned default, 1 each thread's neighbour lines
+   * by per-thread asynchronous copies, 2 the neighbours' whole field arrays
+   * by bulk copies */
+  int32_t nb_staging;
 } ew_options;
 
 typedef struct ew_ctx ew_ctx;
@@ -358,6 +363,10 @@ int64_t ew_batch_kernel_launches(const ew_batch* batch);
  * the autotuner (exwave_gb300/autotune.py).  No reference counterpart. */
 int ew_tune_set(int32_t dim, int32_t degree, int32_t precision, int32_t cells_per_block);
 int32_t ew_tune_get(int32_t dim, int32_t degree, int32_t precision);
+/* The same table's neighbour staging (ew_options.nb_staging; 0 restores the
+ * built-in choice). */
+int ew_tune_set_staging(int32_t dim, int32_t degree, int32_t precision, int32_t nb_staging);
+int32_t ew_tune_get_staging(int32_t dim, int32_t degree, int32_t precision);
 
 /* Waits for the context's stream and reports a raised device error flag. */
 int ew_synchronize(ew_ctx* ctx);
