@@ -63,6 +63,8 @@ def parse():
                          "error; mixed: FP32 operator; mixed_ff: compensated (float-float) operator")
     ap.add_argument("--cells-per-block", type=int, default=0,
                     help="cells per thread block of the operator kernel (0: tuned value)")
+    ap.add_argument("--nb-staging", type=int, default=0,
+                    help="line kernel's neighbour layout: 0 tuned, 1 per-thread lines, 2 bulk arrays")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -638,7 +640,8 @@ def main():
     with ClockSampler(local) as clk:
         for prec in order:
             o = ew.WaveEquationOperation(m, args.degree, precision=prec, device=local,
-                                         cells_per_block=args.cells_per_block)
+                                         cells_per_block=args.cells_per_block,
+                                         nb_staging=args.nb_staging)
             ms, launches, errs, _ = time_steps(o, dt, args.steps, args.warmup, torch, barrier)
             ms = rep.max(ms)  # the slowest replica times the whole job
             n = o.n_dofs

@@ -96,8 +96,17 @@ def run(dims=(2, 3), degrees=range(1, 8), precisions=("mixed", "mixed_ff", "fp64
     return entries
 
 
-def save(entries, gpu_name):
+def save(entries, gpu_name, merge=False):
+    """Write the table; with merge, entries of other (dim, degree, precision)
+    already in the table are kept."""
     os.makedirs(os.path.dirname(TABLE), exist_ok=True)
+    if merge and os.path.exists(TABLE):
+        with open(TABLE) as f:
+            old = json.load(f).get("entries", [])
+        key = lambda e: (e["dim"], e["degree"], e["precision"])
+        new_keys = {key(e) for e in entries}
+        entries = [e for e in old if key(e) not in new_keys] + entries
+        entries.sort(key=lambda e: (e["dim"], e["degree"], e["precision"]))
     with open(TABLE, "w") as f:
         json.dump({"gpu": gpu_name, "entries": entries}, f, indent=1)
 
@@ -107,12 +116,15 @@ def main():
     ap.add_argument("--target-dofs", type=float, default=4e7)
     ap.add_argument("--dims", default="2,3")
     ap.add_argument("--precisions", default="mixed,mixed_ff,fp64")
+    ap.add_argument("--degrees", default="1,7", help="degree range (inclusive)")
+    ap.add_argument("--merge", action="store_true", help="keep the table's other entries")
     args = ap.parse_args()
     import torch
     _lib.load()
-    entries = run(dims=[int(d) for d in args.dims.split(",")],
+    lo, hi = (int(x) for x in args.degrees.split(","))
+    entries = run(dims=[int(d) for d in args.dims.split(",")], degrees=range(lo, hi + 1),
                   precisions=args.precisions.split(","), target_dofs=args.target_dofs)
-    save(entries, torch.cuda.get_device_name(0))
+    save(entries, torch.cuda.get_device_name(0), merge=args.merge)
     print("wrote", TABLE)
 
 
