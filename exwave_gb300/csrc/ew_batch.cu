@@ -16,8 +16,10 @@
 // unevaluated float pair: FP32 hi in the stage input buffer X[cur] and FP32
 // lo in U[1] (about 48 significant bits).  The first stage of a step reads
 // hi and lo like a middle stage reads its input, the accumulator lives in
-// U[0] during the step and the last stage writes the new hi and lo.
-// Receivers, get_state and set_state convert between the pair and FP64.
+// U[0] during the step and the last stage writes the new hi and lo.  The
+// compensated precision keeps it as interleaved float pairs in U[cur] (8
+// bytes, like FP64), read by the next first stage as input and accumulator.
+// Receivers, get_state and set_state convert between the pairs and FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -150,8 +152,18 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity, int32_t* f
     const size_t p0 = ((size_t)cell * r.F + r.dim) * r.N;
     const double* w = r.rec_w + (size_t)k * r.N;
     double acc = 0.0;
-    for (int q = lane; q < r.N; q += 32)
-      acc += w[q] * (r.mixed ? (double)hi[p0 + q] + (double)r.L[p0 + q] : state[p0 + q]);
+    for (int q = lane; q < r.N; q += 32) {
+      double v;
+      if (r.mixed == 1) {
+        v = (double)hi[p0 + q] + (double)r.L[p0 + q];
+      } else if (r.mixed == 2) {
+        const float2 pr = reinterpret_cast<const float2*>(state)[p0 + q];
+        v = (double)pr.x + (double)pr.y;
+      } else {
+        v = state[p0 + q];
+      }
+      acc += w[q] * v;
+    }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) {
       if (record) r.trace[step * r.n_rec + k] = acc;
@@ -164,6 +176,21 @@ __global__ void receiver_kernel(const RecDesc* rd, int n, int parity, int32_t* f
     if (record) r.clock[1] = (double)(step + 1);
     if (bad) r.clock[3] = 1.0;
     flags[s] = r.clock[3] != 0.0 ? 1 : 0;
+  }
+}
+
+// Interleaved float pairs <-> FP64 state (compensated batches).
+__global__ void join_pairs_kernel(const float2* pr, int64_t n, double* state) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    state[i] = (double)pr[i].x + (double)pr[i].y;
+}
+__global__ void split_pairs_kernel(const double* state, int64_t n, float2* pr) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float h, l;
+    ew::f64_split(state[i], h, l);
+    pr[i] = make_float2(h, l);
   }
 }
 
@@ -353,10 +380,10 @@ void stage_descs(const ew_batch* b, const Solve& s, int parity, ew::SolveDesc* o
   void* Xo[5];
   double* Ao[5];
   if (b->ff) {
-    // compensated: FP64 state in U[parity] read by the first stage (X == A),
-    // float-pair accumulator in U[1 - parity], float-pair stage inputs
-    // alternating in X[0] / X[1]; the last stage leaves the FP64 state in
-    // U[1 - parity]
+    // compensated: float-pair state in U[parity] read by the first stage
+    // (X == A), float-pair accumulator in U[1 - parity], float-pair stage
+    // inputs alternating in X[0] / X[1]; the last stage leaves the new state's
+    // pairs in U[1 - parity]
     void* Y0 = s.X[0];
     void* Y1 = s.X[1];
     X[0] = Nv; A[0] = Nv; Xo[0] = Y0; Ao[0] = Pv;
@@ -440,8 +467,11 @@ int rebuild(ew_batch* b) {
     const int F = g.dim + 1;
     for (int st = 0; st < 5; ++st) {
       if (b->ff) {
-        g.variant[st] = st == 0 ? ew::CV_FF_S1 : (st < 4 ? ew::CV_FF_MID : ew::CV_FF_LAST);
-        g.sx[st] = (st == 0) ? 0 : 1;  // first stage: X is the FP64 state (the accumulator)
+        // the state is kept as float pairs: the first stage reads it as input
+        // and accumulator at once (middle-stage kernel, X == A), the last one
+        // writes the new pairs
+        g.variant[st] = st < 4 ? ew::CV_FF_MID : ew::CV_FF_LAST_PAIR;
+        g.sx[st] = (st == 0) ? 0 : 1;
       } else if (b->mixed) {
         g.variant[st] = st == 0 ? ew::CV_MIX_S1_FF : (st < 4 ? ew::CV_MIX_MID : ew::CV_MIX_LAST_FF);
         g.sx[st] = 1;
@@ -504,7 +534,8 @@ int rebuild(ew_batch* b) {
       r.H[0] = static_cast<const float*>(s.X[0]);
       r.H[1] = static_cast<const float*>(s.X[1]);
       r.L = reinterpret_cast<const float*>(s.U[1]);
-      r.mixed = b->mixed && !b->ff ? 1 : 0;  // float-pair state between steps
+      // state between steps: FP64 (0), FP32 hi and lo arrays (1), interleaved pairs (2)
+      r.mixed = b->ff ? 2 : (b->mixed ? 1 : 0);
       r.pad = 0;
       r.rec_w = s.rec_w;
       r.rec_cell = s.rec_cell;
@@ -846,6 +877,12 @@ int ew_batch_set_state(ew_batch* b, int32_t id, const double* state) {
     split_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
         state, s->n_dofs, static_cast<float*>(s->X[s->cur]), reinterpret_cast<float*>(s->U[1]));
     e = cudaGetLastError();
+  } else if (b->ff) {
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
+    split_pairs_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
+        state, s->n_dofs, reinterpret_cast<float2*>(s->U[s->cur]));
+    e = cudaGetLastError();
   } else {
     e = cudaMemcpyAsync(s->U[s->cur], state, (size_t)s->n_dofs * 8, cudaMemcpyDeviceToDevice,
                         b->stream);
@@ -865,6 +902,12 @@ int ew_batch_get_state(ew_batch* b, int32_t id, double* state) {
     join_state_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
         static_cast<const float*>(s->X[s->cur]), reinterpret_cast<const float*>(s->U[1]), s->n_dofs,
         state);
+    e = cudaGetLastError();
+  } else if (b->ff) {
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((s->n_dofs + threads - 1) / threads, 1 << 20);
+    join_pairs_kernel<<<(unsigned)blocks, threads, 0, b->stream>>>(
+        reinterpret_cast<const float2*>(s->U[s->cur]), s->n_dofs, state);
     e = cudaGetLastError();
   } else {
     e = cudaMemcpyAsync(state, s->U[s->cur], (size_t)s->n_dofs * 8, cudaMemcpyDeviceToDevice,

@@ -104,14 +104,20 @@ def test_batch_matches_single_context(env, precision):
     b.set_state(sid, u0)
     b.step(4)
     vn, vnp = u0.clone(), torch.zeros_like(u0)
-    for _ in range(4):
-        op.lsrk45_step(dt, vn, vnp)
-        vn, vnp = vnp, vn
+    if precision == "mixed_ff":
+        # one multi-step call: the state as float pairs between steps, like
+        # the batch
+        op.lsrk45_steps(dt, 4, vn, vnp)
+        vn = vnp
+    else:
+        for _ in range(4):
+            op.lsrk45_step(dt, vn, vnp)
+            vn, vnp = vnp, vn
     op.synchronize()
     b.synchronize()
     got = b.get_state(sid, torch.zeros_like(u0))
     if precision in ("fp64", "mixed_ff"):
-        # the same kernels on the same FP64 state between steps: bit-identical
+        # the same kernels on the same state between steps: bit-identical
         assert torch.equal(got, vn)
     else:
         # the batch carries the state's FP32 split between steps and runs
