@@ -577,8 +577,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
   const int nstride = blockDim.x;
   // With bulk copies usable, the same area holds whole neighbour field
   // arrays instead: slot (cell * 2 DIM + face) * 2 + (u_e, p), each filled by
-  // one bulk copy of the array rounded out to 16-byte boundaries, issued by
-  // warp 0 and completed on bars[3].  Bulk copies are enabled only when a
+  // one bulk copy of the array rounded out to 16-byte boundaries, completed
+  // on bars[3].  Bulk copies are enabled only when a
   // cell's data is a multiple of 16 bytes, so that the rounded windows stay
   // inside the stage input array.
   constexpr int NB_SLOT = CartSmem<DIM, NP, Real, InT, A_ELEM>::NB_SLOT;
@@ -588,7 +588,6 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
   auto nb_rem = [](int nb, int f) -> int {
     return (int)((((size_t)nb * F + f) * N * sizeof(InT)) & 15);
   };
-  const unsigned w0mask = blockDim.x >= 32 ? 0xffffffffu : ((1u << blockDim.x) - 1u);
   // the neighbours of this thread's line (both sides); boundary: -id
   auto lookup_nb = [&](const WorkItem& wi, const SolveDesc& sd, int* nbs) {
     nbs[0] = nbs[1] = -EW_BC_HARD_WALL_ID;
@@ -605,13 +604,15 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
       }
     }
   };
-  // warp 0: the item's neighbour arrays outside the block, one (cell, face)
-  // pair per lane and round of 32; each round's bytes are announced before
-  // its copies, and one arrival after the last round ends the phase
-  auto issue_nb = [&](const WorkItem& wi, const SolveDesc& sd) {
-    const int lane = threadIdx.x;
-    const int pairs = wi.n_cells * 2 * DIM;
-    const unsigned char* Xg = static_cast<const unsigned char*>(sd.X);
+  // The item's neighbour arrays outside the block, issued by the first
+  // thread of every (cell, direction) of the block (spread over the warps):
+  // it copies the arrays of the two faces its direction's lines meet, whose
+  // neighbour ids lookup_nb has just loaded.  bars[3] expects one arrival
+  // from each of these CB * DIM threads per item (cells beyond a partial
+  // item arrive without copies); each announces its bytes before its copies.
+  const bool nb_issuer = tt == 0;
+  auto issue_nb = [&](const WorkItem& wi, const int* nbs) {
+    if (!nb_issuer) return;
     constexpr size_t fbytes = (size_t)N * sizeof(InT);
     // the 16-byte window around field f of cell nb: start and length
     auto window = [&](int nb, int f, size_t& w0) -> uint32_t {
@@ -619,30 +620,33 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
       w0 = s0 & ~(size_t)15;
       return (uint32_t)(((s0 + fbytes + 15) & ~(size_t)15) - w0);
     };
-    for (int q0 = 0; q0 < pairs; q0 += 32) {
-      const int q = q0 + lane;
-      int nb = -1;
-      if (q < pairs) {
-        nb = sd.nbr[(size_t)(wi.cell_begin + q / (2 * DIM)) * 2 * DIM + q % (2 * DIM)];
+    const SolveDesc* sdp = La.solves ? La.solves + wi.solve : &La.single;
+    const unsigned char* Xg = static_cast<const unsigned char*>(sdp->X);
+    size_t wu[2] = {0, 0}, wp[2] = {0, 0};
+    uint32_t lu[2] = {0, 0}, lp[2] = {0, 0};
+    uint32_t bytes = 0;
+    if (tcl < wi.n_cells) {
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const int nb = nbs[s];
         const int nl = nb - wi.cell_begin;
-        if (!(nb >= 0 && nb < sd.n_cells && !(nl >= 0 && nl < wi.n_cells))) nb = -1;
-      }
-      size_t wu = 0, wp = 0;
-      uint32_t lu = 0, lp = 0;
-      if (nb >= 0) {
-        lu = window(nb, (q % (2 * DIM)) / 2, wu);
-        lp = window(nb, DIM, wp);
-      }
-      const uint32_t bytes = __reduce_add_sync(w0mask, lu + lp);
-      if (lane == 0 && bytes > 0) mbar_add_tx(&bars[3], bytes);
-      __syncwarp(w0mask);
-      if (nb >= 0) {
-        bulk_g2s(sNb + (size_t)(2 * q) * NB_SLOT, Xg + wu, lu, &bars[3]);
-        bulk_g2s(sNb + (size_t)(2 * q + 1) * NB_SLOT, Xg + wp, lp, &bars[3]);
+        if (nb >= 0 && !(nl >= 0 && nl < wi.n_cells)) {
+          lu[s] = window(nb, te, wu[s]);
+          lp[s] = window(nb, DIM, wp[s]);
+          bytes += lu[s] + lp[s];
+        }
       }
     }
-    __syncwarp(w0mask);
-    if (lane == 0) mbar_arrive(&bars[3]);
+    if (bytes > 0) mbar_add_tx(&bars[3], bytes);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      if (lu[s] > 0) {
+        const int q = tcl * 2 * DIM + 2 * te + s;
+        bulk_g2s(sNb + (size_t)(2 * q) * NB_SLOT, Xg + wu[s], lu[s], &bars[3]);
+        bulk_g2s(sNb + (size_t)(2 * q + 1) * NB_SLOT, Xg + wp[s], lp[s], &bars[3]);
+      }
+    }
+    mbar_arrive(&bars[3]);
   };
   // Neighbour lines (u_e and p, both sides) of item wi that are not in the
   // item's own block: asynchronous copies from L2 into this thread's slot.
@@ -670,7 +674,7 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     mbar_init(&bars[2], 1);
-    mbar_init(&bars[3], 1);
+    mbar_init(&bars[3], CB * DIM);
     fence_barrier_init();
   }
   __syncthreads();
@@ -681,7 +685,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
   int it = 0;
   bool prev_a_ok = true;  // the previous item's accumulator copy arrived
   bool prev_nb_ok = true;  // this thread saw the previous item's neighbour arrays arrive
-  int nb_last = -1;        // warp 0: item index of the last neighbour phase issued
+  int nb_last = -1;        // item index of the last neighbour phase issued
+  bool nb_fail = false;    // a neighbour wait of the previous item gave up
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x, ++it) {
     const int b = it & 1;
     const bool has_next = w + (int)gridDim.x < La.n_work;
@@ -731,9 +736,10 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
     // phase, measured 3-4% slower)
     if (nb_bulk) {
       lookup_nb(wi, sd, nbs);
-      // a new phase only once every lane of warp 0 saw the previous one end
-      if (threadIdx.x < 32 && __all_sync(w0mask, prev_nb_ok)) {
-        issue_nb(wi, sd);
+      // a new phase only once every wait of the previous one ended in time
+      // (known to every thread from the previous item's last barrier)
+      if (!nb_fail) {
+        issue_nb(wi, nbs);
         nb_last = it;
       }
     } else {
@@ -1194,7 +1200,8 @@ __global__ void __maxnreg__(is_f64_v<Real> ? 96 : (is_ff_v<Real> ? EW_FF_MAXNREG
         }
       }
     }
-    __syncthreads();
+    // every wait on this item's neighbour arrays has ended here
+    nb_fail = __syncthreads_or(!prev_nb_ok) != 0;
     // ---------------------------------------------------------- pressure
     const int src_local = sd.src_cell - wi.cell_begin;
     Real src_val = Real(0);
