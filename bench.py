@@ -42,7 +42,7 @@ STAGES = 5
 # what each precision stores and computes in
 DTYPES = {
     "mixed": "f32-operator/f32-stage-input/float-pair-state-in-multi-step-calls/f64-state-at-call-boundary",
-    "mixed_ff": "ff-operator(~44-bit)/float-pair-stage-input/f64-state",
+    "mixed_ff": "ff-operator(~44-bit)/float-pair-stage-input/float-pair-state-in-multi-step-calls/f64-state-at-call-boundary",
     "fp64": "f64",
 }
 # algorithmic bytes per DoF and LSRK45 step: each vector once per stage at
