@@ -94,7 +94,9 @@ struct StageK {
 
 template <typename Real, typename InT, typename OutT, bool CART, bool POST, bool SPEC = true>
 struct CkK {
-  static size_t smem(int cb) { return (size_t)CkSmem<DIM, NP, CART>(cb).end * sizeof(Real); }
+  static size_t smem(int cb) {
+    return (size_t)CkSmem<DIM, NP, CART>(cb, ck_in_words<Real, InT>()).end * sizeof(Real);
+  }
   static cudaError_t launch(const LaunchArgs& a, int grid, cudaStream_t st) {
     const int cb = a.cells_per_block;
     return run(ck_kernel<DIM, NP, Real, InT, OutT, CART, POST, SPEC>, a, grid, cb * N, smem(cb), st);

@@ -57,8 +57,10 @@ template <int DIM, int NP, bool CART>
 struct CkSmem {
   using S = Shape<DIM, NP, CART>;
   OpSmem<DIM, NP, CART> op;
-  int Sv, T1, T2, C[8], J, end;
-  __host__ __device__ explicit CkSmem(int CB) : op(CB) {
+  int Sv, T1, T2, C[8], J, P, PG, PM, end;
+  // in_words: Real-sized words per stored input value (2 for FP64 input to
+  // the FP32 kernel, else 1)
+  __host__ __device__ CkSmem(int CB, int in_words) : op(CB) {
     // J: inverse-transpose Jacobians at the level-0 points, [cell][DIM*DIM][point]
     J = op.end;
     Sv = J + (CART ? 0 : CB * DIM * DIM * S::N);
@@ -70,7 +72,12 @@ struct CkSmem {
       C[r] = o;
       o += CB * S::F * ipow_c(NP - 2 * r, DIM);
     }
-    end = (o + 3) & ~3;
+    // P, PG, PM: the next work item's input values (as stored), geometry and
+    // materials, copied asynchronously while the current item is computed
+    P = (o + 3) & ~3;
+    PG = P + CB * S::F * S::N * in_words;
+    PM = PG + CB * S::GEO;
+    end = (PM + CB * 4 + 3) & ~3;
   }
 };
 
@@ -696,6 +703,12 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Acc* c0) {
   }
 }
 
+// Real-sized words per stored input value (staging area of the CK kernel)
+template <typename Real, typename InT>
+constexpr int ck_in_words() {
+  return (int)((sizeof(InT) + sizeof(Real) - 1) / sizeof(Real));
+}
+
 template <int DIM, int NP, typename Real, typename InT, typename OutT, bool CART, bool POST,
           bool SPEC = true>
 __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const LaunchArgs La) {
@@ -708,7 +721,7 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real* sm = reinterpret_cast<Real*>(smem_raw);
   const int CB = La.cells_per_block;
-  const CkSmem<DIM, NP, CART> lay(CB);
+  const CkSmem<DIM, NP, CART> lay(CB, ck_in_words<Real, InT>());
   Real* sB = sm + lay.op.basis;
   Real* sX = sm + lay.op.X;
   Real* sG = sm + lay.op.G;
@@ -742,12 +755,38 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     half_dt2 = La.ck_half_dt2;
   }
 
+  // Work items are pipelined: the next item's inputs, geometry and
+  // materials are copied asynchronously (cp.async, one value per copy) into
+  // the staging area while the current item is computed, and converted into
+  // the compute layout when its turn comes.
+  const InT* sPX = reinterpret_cast<const InT*>(sm + lay.P);
+  auto prefetch = [&](int wn) {
+    const WorkItem wj = La.work[wn];
+    const SolveDesc sdn = pick(La, wj.solve);
+    const int tot = wj.n_cells * F * N;
+    const InT* X = static_cast<const InT*>(sdn.X) + (size_t)wj.cell_begin * F * N;
+    InT* px = reinterpret_cast<InT*>(sm + lay.P);
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) cp_async<sizeof(InT)>(px + i, X + i);
+    const Real* G = static_cast<const Real*>(sdn.geo) + (size_t)wj.cell_begin * S::GEO;
+    for (int i = threadIdx.x; i < wj.n_cells * S::GEO; i += blockDim.x)
+      cp_async<sizeof(Real)>(sm + lay.PG + i, G + i);
+    const Real* M = static_cast<const Real*>(sdn.mat) + (size_t)wj.cell_begin * 4;
+    for (int i = threadIdx.x; i < wj.n_cells * 4; i += blockDim.x) cp_async<sizeof(Real)>(sm + lay.PM + i, M + i);
+    cp_async_commit();
+  };
+  if ((int)blockIdx.x < La.n_work) prefetch(blockIdx.x);
+
   for (int w = blockIdx.x; w < La.n_work; w += gridDim.x) {
     const WorkItem wi = La.work[w];
     const SolveDesc sd = pick(La, wi.solve);
     const int nc = wi.n_cells;
+    cp_async_wait_all();
+    // the previous item is done with the compute layout; this item's staged
+    // values (every thread's copies) are visible
     __syncthreads();
-    load_block<DIM, NP, Real, InT, CART>(sd, wi.cell_begin, nc, sX, sGeo, sMat);
+    for (int i = threadIdx.x; i < nc * F * N; i += blockDim.x) sX[i] = to_real<Real>(sPX[i]);
+    for (int i = threadIdx.x; i < nc * S::GEO; i += blockDim.x) sGeo[i] = sm[lay.PG + i];
+    for (int i = threadIdx.x; i < nc * 4; i += blockDim.x) sMat[i] = sm[lay.PM + i];
     for (int r = 1; r < NL; ++r) {
       const int sz = nc * F * ipow_rt(NP - 2 * r, DIM);
       for (int i = threadIdx.x; i < sz; i += blockDim.x) sm[lay.C[r] + i] = Real(0);
@@ -810,13 +849,12 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
     using Acc = CkAcc<Real>;
     Acc c0[F];
     if (active) {
-      const size_t gq = ((size_t)wi.cell_begin + cl) * F * N + q;
 #pragma unroll
       for (int fld = 0; fld < F; ++fld) {
         if constexpr (is_ff_v<Acc> && !is_ff_v<Real>) {
           float uh, ul;
           if constexpr (is_f64_v<InT>) {
-            f64_split(load_nc(static_cast<const double*>(sd.X) + gq + fld * N), uh, ul);
+            f64_split(sPX[cl * F * N + fld * N + q], uh, ul);
           } else {
             uh = sX[cl * F * N + fld * N + q];
             ul = 0.f;
@@ -830,6 +868,8 @@ __global__ void __maxnreg__(sizeof(Real) == 8 ? 128 : 80) ck_kernel(const Launch
       }
     }
     __syncthreads();
+    // every read of the staging area is done: the next item may land there
+    if (w + (int)gridDim.x < La.n_work) prefetch(w + gridDim.x);
     CkState<Real> st;
     st.sB = sB;
     st.sS = sS;
