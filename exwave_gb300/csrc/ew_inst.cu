@@ -1,6 +1,7 @@
 // ew_inst.cu -- instantiates the kernels for one (dimension, points per
 // direction) pair, selected by -DEW_DIM and -DEW_NP, and exports their
 // launchers through a table (one object file per pair, compiled in parallel).
+#include "ew_basis.h"
 #include "ew_cart.cuh"
 #include "ew_kernels.cuh"
 #include "ew_launch.h"
@@ -157,7 +158,23 @@ cudaError_t set_constants(const double* w, const double* D, const double* L0, co
   e = cudaMemcpyToSymbol(c_cart_ff, &cff, sizeof(cff));
   if (e != cudaSuccess) return e;
   const FfBounds fb = make_ff_bounds(cd);
-  return cudaMemcpyToSymbol(c_ff_bounds, &fb, sizeof(fb));
+  e = cudaMemcpyToSymbol(c_ff_bounds, &fb, sizeof(fb));
+  if (e != cudaSuccess) return e;
+  // the CK kernel's multilevel tables, in each compute type
+  static_assert(basis_total(NP) <= kCkBasisMax, "CK table larger than its constant array");
+  const std::vector<double> bt = basis_table(NP);
+  if ((int)bt.size() != basis_total(NP)) return cudaErrorInvalidValue;
+  std::vector<float> btf(bt.size());
+  std::vector<FF> btff(bt.size());
+  for (size_t i = 0; i < bt.size(); ++i) {
+    btf[i] = static_cast<float>(bt[i]);
+    btff[i] = FF::from_double(bt[i]);
+  }
+  e = cudaMemcpyToSymbol(c_ckb_d, bt.data(), bt.size() * sizeof(double));
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyToSymbol(c_ckb_f, btf.data(), btf.size() * sizeof(float));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_ckb_ff, btff.data(), btff.size() * sizeof(FF));
 }
 
 template <class K>

@@ -487,9 +487,35 @@ __global__ void __launch_bounds__(512) stage_kernel(const LaunchArgs La) {
 // One sweep of a 1D matrix Mtx (ROWS x COLS, COLS = input extent along DIR)
 // along direction DIR over the tensors of nc cells x nf fields; input
 // extents I0 x I1 x I2, compile-time, per-cell strides cs_in / cs_out.
-template <int DIM, typename Real, int DIR, int ROWS, int I0, int I1, int I2>
-__device__ __forceinline__ void sweep_ct(const Real* Mtx, const Real* in, int cs_in, Real* out,
-                                         int cs_out, int nc, int nf) {
+// The CK kernel's multilevel 1-D tables (basis_table: points, weights,
+// derivative, traces, and the projection and interpolation matrices of
+// every level) in constant memory, one copy per compute type, filled for
+// the unit's point count by set_constants.  The degree-reduction and
+// interpolation sweeps read their matrix entries here at compile-time
+// offsets, as constant operands of the multiply-adds.
+constexpr int kCkBasisMax = 1368;  // basis_total(13)
+namespace {
+__constant__ float c_ckb_f[kCkBasisMax];
+__constant__ double c_ckb_d[kCkBasisMax];
+__constant__ FF c_ckb_ff[kCkBasisMax];
+}  // namespace
+template <typename Real>
+__device__ __forceinline__ const Real* ck_basis_const() {
+  if constexpr (is_f64_v<Real>)
+    return c_ckb_d;
+  else if constexpr (is_ff_v<Real>)
+    return c_ckb_ff;
+  else
+    return c_ckb_f;
+}
+
+// The 1-D matrix at offset MOFF of the constant table (ROWS x COLS, row
+// major) applied along direction DIR of every field of every cell:
+// in (I0 x I1 x I2 points) -> out (ROWS points along DIR).  One thread per
+// (cell, field, line): the line's COLS inputs are read once and its ROWS
+// outputs summed in the order j = 0..COLS-1.
+template <int DIM, typename Real, int DIR, int ROWS, int I0, int I1, int I2, int MOFF>
+__device__ __forceinline__ void sweep_ct(const Real* in, int cs_in, Real* out, int cs_out, int nc, int nf) {
   constexpr int O0 = DIR == 0 ? ROWS : I0;
   constexpr int O1 = DIR == 1 ? ROWS : I1;
   constexpr int O2 = DIR == 2 ? ROWS : I2;
@@ -497,41 +523,53 @@ __device__ __forceinline__ void sweep_ct(const Real* Mtx, const Real* in, int cs
   constexpr int TOUT = O0 * (DIM > 1 ? O1 : 1) * (DIM > 2 ? O2 : 1);
   constexpr int COLS = DIR == 0 ? I0 : (DIR == 1 ? I1 : I2);
   constexpr int SIN = DIR == 0 ? 1 : (DIR == 1 ? I0 : I0 * I1);
-  for (int idx = threadIdx.x; idx < nc * nf * TOUT; idx += blockDim.x) {
-    const int cf = idx / TOUT;  // cell * nf + field
-    const int p = idx - cf * TOUT;
+  constexpr int SOUT = DIR == 0 ? 1 : (DIR == 1 ? O0 : O0 * O1);
+  // the two other directions: a (the faster one) and b, extents and strides
+  constexpr int NA = DIR == 0 ? I1 : I0;
+  constexpr int NB = DIM > 2 ? (DIR == 2 ? I1 : I2) : 1;
+  constexpr int SAI = DIR == 0 ? I0 : 1, SAO = DIR == 0 ? O0 : 1;
+  constexpr int SBI = DIR == 2 ? I0 : I0 * I1, SBO = DIR == 2 ? O0 : O0 * O1;
+  constexpr int NLN = NA * NB;
+  static_assert(MOFF + ROWS * COLS <= kCkBasisMax, "matrix outside the constant table");
+  const Real* Mtx = ck_basis_const<Real>() + MOFF;
+  for (int task = threadIdx.x; task < nc * nf * NLN; task += blockDim.x) {
+    const int cf = task / NLN;  // cell * nf + field
+    const int l = task - cf * NLN;
     const int cl = cf / nf;
     const int fld = cf - cl * nf;
-    const int o0 = p % O0;
-    const int o1 = DIM > 1 ? (p / O0) % O1 : 0;
-    const int o2 = DIM > 2 ? p / (O0 * O1) : 0;
-    const int base = (DIR == 0 ? 0 : o0) + (DIR == 1 ? 0 : o1 * I0) + (DIR == 2 ? 0 : o2 * I0 * I1);
-    const int od = DIR == 0 ? o0 : (DIR == 1 ? o1 : o2);
-    const Real* src = in + cl * cs_in + fld * TIN + base;
-    const Real* mrow = Mtx + od * COLS;
-    Real s = Real(0);
+    const int la = l % NA, lb = l / NA;
+    const Real* src = in + cl * cs_in + fld * TIN + la * SAI + lb * SBI;
+    Real* dst = out + cl * cs_out + fld * TOUT + la * SAO + lb * SBO;
+    Real x[COLS];
 #pragma unroll
-    for (int j = 0; j < COLS; ++j) s += mrow[j] * src[j * SIN];
-    out[cl * cs_out + fld * TOUT + p] = s;
+    for (int j = 0; j < COLS; ++j) x[j] = src[j * SIN];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      Real acc = Real(0);
+#pragma unroll
+      for (int j = 0; j < COLS; ++j) acc += Mtx[r * COLS + j] * x[j];
+      dst[r * SOUT] = acc;
+    }
   }
 }
 
-// A 1D matrix (ROWS x COLS) applied in all DIM directions: src (COLS^DIM
-// points) -> dst (ROWS^DIM points); t1, t2 scratch.  Contains barriers.
-template <int DIM, typename Real, int ROWS, int COLS>
-__device__ __forceinline__ void tensor_ct(const Real* Mtx, const Real* src, int cs_src, Real* dst,
-                                          int cs_dst, Real* t1, Real* t2, int cs_t, int nc, int nf) {
+// The 1-D matrix at offset MOFF of the constant table (ROWS x COLS) applied
+// in all DIM directions: src (COLS^DIM points) -> dst (ROWS^DIM points); t1,
+// t2 scratch.  Contains barriers.
+template <int DIM, typename Real, int ROWS, int COLS, int MOFF>
+__device__ __forceinline__ void tensor_ct(const Real* src, int cs_src, Real* dst, int cs_dst, Real* t1,
+                                          Real* t2, int cs_t, int nc, int nf) {
   if constexpr (DIM == 2) {
-    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, 1>(Mtx, src, cs_src, t1, cs_t, nc, nf);
+    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, 1, MOFF>(src, cs_src, t1, cs_t, nc, nf);
     __syncthreads();
-    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, 1>(Mtx, t1, cs_t, dst, cs_dst, nc, nf);
+    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, 1, MOFF>(t1, cs_t, dst, cs_dst, nc, nf);
     __syncthreads();
   } else {
-    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, COLS>(Mtx, src, cs_src, t1, cs_t, nc, nf);
+    sweep_ct<DIM, Real, 0, ROWS, COLS, COLS, COLS, MOFF>(src, cs_src, t1, cs_t, nc, nf);
     __syncthreads();
-    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, COLS>(Mtx, t1, cs_t, t2, cs_t, nc, nf);
+    sweep_ct<DIM, Real, 1, ROWS, ROWS, COLS, COLS, MOFF>(t1, cs_t, t2, cs_t, nc, nf);
     __syncthreads();
-    sweep_ct<DIM, Real, 2, ROWS, ROWS, ROWS, COLS>(Mtx, t2, cs_t, dst, cs_dst, nc, nf);
+    sweep_ct<DIM, Real, 2, ROWS, ROWS, ROWS, COLS, MOFF>(t2, cs_t, dst, cs_dst, nc, nf);
     __syncthreads();
   }
 }
@@ -668,8 +706,9 @@ __device__ __forceinline__ void ck_steps(CkState<Real>& st, const Real* fac, Acc
   __syncthreads();
   if constexpr (S + 1 < NSTEPS) {
     if constexpr (SPEC && S % 2 == 1) {
-      const Level<Real> Ln = get_level(st.sB, NP, R + 1);
-      tensor_ct<DIM, Real, M - 2, M>(Ln.P, st.sS, F * N, st.sS, F * N, st.sT1, st.sT2, F * N, st.nc, F);
+      // projection P of level R + 1 ((M - 2) x M)
+      constexpr int POFF = basis_offset(NP, R + 1) + 4 * (M - 2) + (M - 2) * (M - 2);
+      tensor_ct<DIM, Real, M - 2, M, POFF>(st.sS, F * N, st.sS, F * N, st.sT1, st.sT2, F * N, st.nc, F);
     }
     ck_steps<DIM, NP, Real, CART, S + 1, NSTEPS, Acc, SPEC>(st, fac, c0);
   }
@@ -682,9 +721,10 @@ __device__ __forceinline__ void ck_gather(CkState<Real>& st, Acc* c0) {
     constexpr int F = DIM + 1, N = ipow_c(NP, DIM);
     constexpr int M = NP - 2 * R, MP = M + 2;
     constexpr int NMP = ipow_c(MP, DIM);
-    const Level<Real> Lr = get_level(st.sB, NP, R);
+    // interpolation E of level R ((M + 2) x M)
+    constexpr int EOFF = basis_offset(NP, R) + 4 * M + M * M + M * MP;
     Real* up = (DIM == 2) ? st.sT2 : st.sT1;
-    tensor_ct<DIM, Real, MP, M>(Lr.E, st.sm + st.C[R], F * ipow_c(M, DIM), up, F * N, st.sT1, st.sT2,
+    tensor_ct<DIM, Real, MP, M, EOFF>(st.sm + st.C[R], F * ipow_c(M, DIM), up, F * N, st.sT1, st.sT2,
                                 F * N, st.nc, F);
     if constexpr (R - 1 == 0) {
       if (st.active) {
