@@ -30,7 +30,8 @@ EXPORTS = ["ew_create", "ew_destroy", "ew_last_error", "ew_set_stream", "ew_n_do
            "ew_tune_set", "ew_tune_get", "ew_tune_set_staging", "ew_tune_get_staging",
            "ew_lsrk45_step_static", "ew_lsrk45_steps",
            "ew_set_receivers", "ew_sample_receivers", "ew_aderadconfull_step",
-           "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update", "ew_check_wait_timeout"]
+           "ew_l2_error_post_membrane", "ew_lsrk_step", "ew_vec_update", "ew_check_wait_timeout",
+           "ew_lsrk45_step_host", "ew_wait_host_copies"]
 
 
 class EwError(RuntimeError):
@@ -85,6 +86,8 @@ def load():
         "ew_rk_update": (ctypes.c_int, [vp, d, d, i32, dp, dp, dp]),
         "ew_lsrk45_step": (ctypes.c_int, [vp, d, dp, dp]),
         "ew_lsrk45_step_static": (ctypes.c_int, [vp, d, dp, dp]),
+        "ew_lsrk45_step_host": (ctypes.c_int, [vp, d, vp, vp]),
+        "ew_wait_host_copies": (ctypes.c_int, [vp]),
         "ew_lsrk45_steps": (ctypes.c_int, [vp, d, i64, dp, dp]),
         "ew_set_receivers": (ctypes.c_int, [vp, i32, dp]),
         "ew_aderadconfull_step": (ctypes.c_int, [vp, d, dp, dp]),

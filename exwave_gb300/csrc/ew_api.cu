@@ -548,6 +548,9 @@ int grid_for(int64_t n) {
 }  // namespace ew
 
 // ================================================================ context
+// ew_lsrk45_step_host copies the state in this many chunks per direction
+constexpr int kHostChunks = 16;
+
 struct ew_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -593,6 +596,14 @@ struct ew_ctx {
   // (the first also holds du/dt of the post-processing)
   double* d_ad[2] = {nullptr, nullptr};
   double* d_post = nullptr;  // basis data of the post-processing (QGauss(k+2), QGauss(k+3))
+  // ew_lsrk45_step_host: the state's two device vectors, the two copy
+  // streams and the events that order them (created on first use)
+  double* d_hstate[2] = {nullptr, nullptr};
+  cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+  cudaEvent_t ev_entry = nullptr, ev_h2d = nullptr, ev_step = nullptr;
+  cudaEvent_t ev_d2h[kHostChunks] = {};
+  const double* last_host_out = nullptr;  // host output of the previous host step
+  bool d2h_pending = false;
   std::string last_error;
   int64_t launches = 0;
 };
@@ -634,11 +645,21 @@ void free_ctx(ew_ctx* c) {
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
+  if (c->s_d2h) cudaStreamSynchronize(c->s_d2h);
+  if (c->s_h2d) cudaStreamSynchronize(c->s_h2d);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
                   c->d_work_stage, c->d_work_ck, c->d_work_cart, c->d_cellc, c->d_err, c->d_tmp64, c->d_x32[0],
-                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w, c->d_ad[0], c->d_ad[1], c->d_post};
+                  c->d_x32[1], c->d_acc, c->d_l2, c->d_rec_cell, c->d_rec_w, c->d_ad[0], c->d_ad[1], c->d_post,
+                  c->d_hstate[0], c->d_hstate[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  cudaEvent_t evs[] = {c->ev_entry, c->ev_h2d, c->ev_step};
+  for (cudaEvent_t e : evs)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->ev_d2h)
+    if (e) cudaEventDestroy(e);
+  if (c->s_h2d) cudaStreamDestroy(c->s_h2d);
+  if (c->s_d2h) cudaStreamDestroy(c->s_d2h);
   cudaSetDevice(prev);
   delete c;
 }
@@ -1285,6 +1306,78 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
   return lsrk45_stages(ctx, dt, vec_n, vec_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1]);
 }
 
+int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h_vec_np) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!h_vec_n || !h_vec_np) return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step_host: NULL host vector");
+  cudaError_t e = cudaSuccess;
+  if (!ctx->d_hstate[0]) {
+    if ((rc = dev_alloc(ctx, &ctx->d_hstate[0], (size_t)ctx->n_dofs)) ||
+        (rc = dev_alloc(ctx, &ctx->d_hstate[1], (size_t)ctx->n_dofs)))
+      return rc;
+    const unsigned fl = cudaEventDisableTiming;
+    if ((e = cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_entry, fl)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_h2d, fl)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_step, fl)) != cudaSuccess)
+      return cuda_fail(ctx, e, "host step streams");
+    for (cudaEvent_t& ev : ctx->ev_d2h)
+      if ((e = cudaEventCreateWithFlags(&ev, fl)) != cudaSuccess) return cuda_fail(ctx, e, "host step events");
+  }
+  double* d_n = ctx->d_hstate[0];
+  double* d_np = ctx->d_hstate[1];
+  const int64_t n = ctx->n_dofs;
+  const int64_t chunk = (n + kHostChunks - 1) / kHostChunks;
+  // the input chunks that the previous call's output copies are still writing
+  const bool chained = ctx->d2h_pending && h_vec_n == ctx->last_host_out;
+  // host -> device, after the work already on the context stream (the
+  // previous step used d_n as a register) and, chunk by chunk, after the
+  // previous call's copy of the same chunk to the host
+  if ((e = cudaEventRecord(ctx->ev_entry, ctx->stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_entry, 0)) != cudaSuccess)
+    return cuda_fail(ctx, e, "host step ordering");
+  for (int k = 0; k < kHostChunks; ++k) {
+    const int64_t o = k * chunk, m = std::min(chunk, n - o);
+    if (m <= 0) break;
+    if (chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[k], 0)) != cudaSuccess)
+      return cuda_fail(ctx, e, "host step ordering");
+    if ((e = cudaMemcpyAsync(d_n + o, h_vec_n + o, (size_t)m * sizeof(double), cudaMemcpyHostToDevice,
+                             ctx->s_h2d)) != cudaSuccess)
+      return cuda_fail(ctx, e, "host to device copy");
+  }
+  // the step: after every input chunk and after the previous call's output
+  // copies (they read d_np, which the step writes)
+  if ((e = cudaEventRecord(ctx->ev_h2d, ctx->s_h2d)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_h2d, 0)) != cudaSuccess ||
+      (ctx->d2h_pending && (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[kHostChunks - 1], 0)) != cudaSuccess))
+    return cuda_fail(ctx, e, "host step ordering");
+  if ((rc = lsrk45_stages(ctx, dt, d_n, d_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1]))) return rc;
+  // device -> host, chunk by chunk, each chunk's completion recorded
+  if ((e = cudaEventRecord(ctx->ev_step, ctx->stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_step, 0)) != cudaSuccess)
+    return cuda_fail(ctx, e, "host step ordering");
+  for (int k = 0; k < kHostChunks; ++k) {
+    const int64_t o = k * chunk, m = std::min(chunk, n - o);
+    if (m > 0 && (e = cudaMemcpyAsync(h_vec_np + o, d_np + o, (size_t)m * sizeof(double),
+                                      cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess)
+      return cuda_fail(ctx, e, "device to host copy");
+    if ((e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
+      return cuda_fail(ctx, e, "host step ordering");
+  }
+  ctx->last_host_out = h_vec_np;
+  ctx->d2h_pending = true;
+  return EW_OK;
+}
+
+int ew_wait_host_copies(ew_ctx* ctx) {
+  int rc = check(ctx);
+  if (rc) return rc;
+  if (!ctx->d2h_pending) return EW_OK;
+  const cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[kHostChunks - 1], 0);
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "host copy ordering");
+}
+
 int ew_vec_update(ew_ctx* ctx, double alpha, double* y, double beta, const double* x, double gamma,
                   const double* z) {
   int rc = check(ctx);
@@ -1890,6 +1983,8 @@ int ew_synchronize(ew_ctx* ctx) {
   if (rc) return rc;
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+  if (ctx->s_d2h && (e = cudaStreamSynchronize(ctx->s_d2h)) != cudaSuccess)
+    return cuda_fail(ctx, e, "host copy stream synchronize");
   int flags = 0;
   e = cudaMemcpy(&flags, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "error flag readback");

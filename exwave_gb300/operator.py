@@ -111,6 +111,22 @@ class WaveEquationOperation:
     def lsrk45_step(self, dt, vec_n, vec_np):
         self._chk(self.L.ew_lsrk45_step(self.ctx, dt, _ptr(vec_n), _ptr(vec_np)))
 
+    def lsrk45_step_host(self, dt, host_n, host_np):
+        """One LSRK45 step on host (CPU) float64 tensors, pinned for
+        asynchronous copies; host_n and host_np may be the same tensor.  The
+        copies overlap with those of the previous call when its output is
+        this call's input.  host_np is complete after synchronize(), or on
+        the context stream after wait_host_copies()."""
+        for t in (host_n, host_np):
+            if t.is_cuda or not t.is_contiguous() or t.dtype != self.torch.float64 or t.numel() != self.n_dofs:
+                raise ValueError("expected contiguous float64 host tensors of n_dofs entries")
+        self._chk(self.L.ew_lsrk45_step_host(self.ctx, dt, ctypes.c_void_p(host_n.data_ptr()),
+                                             ctypes.c_void_p(host_np.data_ptr())))
+
+    def wait_host_copies(self):
+        """Orders the context stream after the last host step's copies to the host."""
+        self._chk(self.L.ew_wait_host_copies(self.ctx))
+
     LSRK_SCHEMES = {"LSRK33R2": 0, "LSRK45R2": 1, "LSRK59R2": 2}
 
     def lsrk_step(self, scheme, dt, vec_n, vec_np):

@@ -128,6 +128,24 @@ int ew_rk_update(ew_ctx* ctx, double f1, double f2, int32_t is_last, const doubl
  * the reference. */
 int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
 
+/* The same step on HOST vectors, the storage of the reference's
+ * perform_time_step (its LA::distributed::Vector<double> lives in host
+ * memory): h_vec_n is copied to a device vector owned by the context, the
+ * step runs on the context stream, and the new state is copied to h_vec_np
+ * (h_vec_n is not modified unless it is h_vec_np; both may be the same
+ * array).  The copies run in chunks on two internal streams: when a call's
+ * input is the previous call's output, each chunk's host-to-device copy
+ * starts as soon as the previous call's device-to-host copy of that chunk
+ * has landed, so the two directions overlap.  Host arrays should be pinned
+ * (cudaHostAlloc / cudaHostRegister) for the copies to be asynchronous.
+ * Returns once the work is enqueued; h_vec_np is complete after
+ * ew_synchronize, or on the context stream after ew_wait_host_copies. */
+int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h_vec_np);
+/* Orders the context stream after the device-to-host copies of the last
+ * ew_lsrk45_step_host call (an event recorded or a synchronize on the stream
+ * afterwards covers them). */
+int ew_wait_host_copies(ew_ctx* ctx);
+
 /* Low-storage 2-register schemes of the reference, selected by
  * ew_lsrk_scheme: replaces LowStorageRK33Reg2 (time_integrators.cc:200-233),
  * LowStorageRK45Reg2 (:235-283, the same as ew_lsrk45_step) and
