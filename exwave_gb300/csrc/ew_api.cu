@@ -1255,6 +1255,25 @@ namespace {
 // inputs used ping-pong (mixed and compensated paths: FP32 values or float
 // pairs).  Shared by ew_lsrk45_step (scratch owned by the context) and
 // ew_lsrk45_step_static (scratch in the static device array).
+// First LSRK45 stage from the FP64 state in vec_n (input and accumulator at
+// once), new accumulator to acc, next stage input to X0.  Compensated
+// Cartesian path: the state is first split in place into float pairs (vec_n
+// is a register of the step), and the stage runs as the middle-stage kernel
+// on them, like the first stage of a later step in a multi-step call; the
+// values are the same exact splits the FP64-input kernel forms on load, at
+// 0.6 of its cost.  Otherwise the FP64-input kernel.
+int ff_first_stage(ew_ctx* ctx, double* vec_n, double* acc, float* X0, double f1, double f2) {
+  using namespace ew;
+  if (ctx->ff && ctx->line) {
+    const cudaError_t e = launch_split_pairs(vec_n, ctx->n_dofs, vec_n, ctx->stream);
+    ++ctx->launches;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "split to float pairs");
+    return launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, vec_n, vec_n, X0, acc, MODE_RK_MID, f1, f2,
+                        1.0f);
+  }
+  return launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, acc, MODE_RK_MID, f1, f2, 1.0f);
+}
+
 int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double* T, float* X0,
                   float* X1) {
   using namespace ew;
@@ -1284,9 +1303,7 @@ int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double*
   }
   // mixed: accumulator in vec_np (in place; on Cartesian meshes a float-float
   // pair between the stages, FP64 at the end), FP32 stage inputs ping-pong
-  rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0],
-                    f2[0], 1.0f);
-  if (rc) return rc;
+  if ((rc = ff_first_stage(ctx, vec_n, vec_np, X0, f1[0], f2[0]))) return rc;
   const float* xin[4] = {X0, X1, X0, X1};
   float* xout[4] = {X1, X0, X1, nullptr};
   for (int s = 1; s < 5; ++s) {
@@ -1536,8 +1553,7 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
     for (int64_t step = 0; step < n_steps; ++step) {
       const bool last_step = step + 1 == n_steps;
       if (step == 0)
-        rc = launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, st, st, xb[0], ac, MODE_RK_MID, f1[0],
-                          f2[0], 1.0f);
+        rc = ff_first_stage(ctx, st, ac, xb[0], f1[0], f2[0]);
       else
         rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, st, st, xb[0], ac, MODE_RK_MID, f1[0],
                           f2[0], 1.0f);

@@ -194,6 +194,7 @@ __global__ void split_pairs_kernel(const double* state, int64_t n, float2* pr) {
   }
 }
 
+
 // FP32 hi + lo -> FP64 state.
 __global__ void join_state_kernel(const float* hi, const float* lo, int64_t n, double* state) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -231,6 +232,16 @@ std::vector<T> cast_vec(const std::vector<double>& v) {
 }
 
 }  // namespace
+
+namespace ew {
+cudaError_t launch_split_pairs(const double* state, int64_t n, void* pairs, cudaStream_t stream) {
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((n + threads - 1) / threads, 1 << 20);
+  if (blocks < 1) return cudaSuccess;
+  split_pairs_kernel<<<(unsigned)blocks, threads, 0, stream>>>(state, n, static_cast<float2*>(pairs));
+  return cudaGetLastError();
+}
+}  // namespace ew
 
 struct ew_batch {
   int device = 0;

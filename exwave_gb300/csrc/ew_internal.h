@@ -24,6 +24,10 @@ cudaError_t upload_cart_constants(int dim, int np);
 // `polls` tries and raising ERR_WAIT_TIMEOUT in *err (ew_diag.cu).
 cudaError_t launch_wait_timeout(int polls, int* err, cudaStream_t stream);
 
+// FP64 state -> interleaved float pairs (hi, lo: the exact split) in the
+// same 8-byte slots; pairs may be state (in place) (ew_batch.cu).
+cudaError_t launch_split_pairs(const double* state, int64_t n, void* pairs, cudaStream_t stream);
+
 // Tuned cells per block for (dim, degree, precision); 0 when unset.
 int tuned_cells_per_block(int dim, int degree, int precision);
 // Tuned neighbour staging of the line kernel (0 unset, 1 lines, 2 bulk).
