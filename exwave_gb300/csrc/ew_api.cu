@@ -1354,6 +1354,10 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
   if ((e = cudaEventRecord(ctx->ev_entry, ctx->stream)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_entry, 0)) != cudaSuccess)
     return cuda_fail(ctx, e, "host step ordering");
+  // any other input may still overlap the previous output: after all of it
+  if (ctx->d2h_pending && !chained &&
+      (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[kHostChunks - 1], 0)) != cudaSuccess)
+    return cuda_fail(ctx, e, "host step ordering");
   for (int k = 0; k < kHostChunks; ++k) {
     const int64_t o = k * chunk, m = std::min(chunk, n - o);
     if (m <= 0) break;
