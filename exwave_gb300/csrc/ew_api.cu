@@ -580,6 +580,9 @@ struct ew_ctx {
   ew::WorkItem* d_work_cart = nullptr;
   int n_work_cart = 0;
   int cb_cart = 1;
+  // line kernel launches over the work items [wr_begin, wr_begin + wr_count)
+  // only (wr_count < 0: all)
+  int wr_begin = 0, wr_count = -1;
   int grid_stage[ew::N_STAGE_VARIANTS] = {0, 0, 0};
   int grid_ck = 0;
   int* d_err = nullptr;
@@ -602,6 +605,17 @@ struct ew_ctx {
   cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
   cudaEvent_t ev_entry = nullptr, ev_h2d = nullptr, ev_step = nullptr;
   cudaEvent_t ev_d2h[kHostChunks] = {};
+  cudaEvent_t ev_in[kHostChunks] = {};  // input chunk on the device (and split)
+  cudaEvent_t ev_s5[kHostChunks] = {};  // last stage done on the chunk
+  // the chunks: with the line kernel, runs of whole work items, and the
+  // input chunks that hold their cells' neighbours (lo..hi); else equal
+  // runs of DoFs
+  struct HostChunk {
+    int item_begin = 0, n_items = 0;
+    int64_t dof_begin = 0, n_dofs = 0;
+    int lo = 0, hi = 0;
+  };
+  std::vector<HostChunk> hchunks;
   const double* last_host_out = nullptr;  // host output of the previous host step
   bool d2h_pending = false;
   std::string last_error;
@@ -656,8 +670,9 @@ void free_ctx(ew_ctx* c) {
   cudaEvent_t evs[] = {c->ev_entry, c->ev_h2d, c->ev_step};
   for (cudaEvent_t e : evs)
     if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e : c->ev_d2h)
-    if (e) cudaEventDestroy(e);
+  for (int k = 0; k < kHostChunks; ++k)
+    for (cudaEvent_t e : {c->ev_d2h[k], c->ev_in[k], c->ev_s5[k]})
+      if (e) cudaEventDestroy(e);
   if (c->s_h2d) cudaStreamDestroy(c->s_h2d);
   if (c->s_d2h) cudaStreamDestroy(c->s_d2h);
   cudaSetDevice(prev);
@@ -842,12 +857,13 @@ int launch_stage(ew_ctx* c, int variant, int cvar, const double* A, const void* 
     const bool tma = (cell_elems * in_sz) % 16 == 0 && (cell_elems * a_sz) % 16 == 0 &&
                      (reinterpret_cast<uintptr_t>(X) % 16) == 0 &&
                      (!sa || (reinterpret_cast<uintptr_t>(A) % 16) == 0);
-    a.work = c->d_work_cart;
-    a.n_work = c->n_work_cart;
+    // the whole work list, or the range set for a chunked launch
+    a.work = c->d_work_cart + (c->wr_count >= 0 ? c->wr_begin : 0);
+    a.n_work = c->wr_count >= 0 ? c->wr_count : c->n_work_cart;
     a.cells_per_block = c->cb_cart;
     const ew::CartEntry& k = c->kt->cart[cvar];
     const int occ = std::max(1, k.occupancy(c->cb_cart, sx));
-    const int grid = std::max(1, std::min(c->n_work_cart, occ * c->num_sms));
+    const int grid = std::max(1, std::min(a.n_work, occ * c->num_sms));
     e = k.launch(a, sx, tma ? 1 : 0, c->nb_lines ? 1 : 0, grid, c->stream);
   } else {
     const ew::KernelEntry& k = c->kt->stage[variant][c->cart ? 1 : 0];
@@ -1255,32 +1271,32 @@ namespace {
 // inputs used ping-pong (mixed and compensated paths: FP32 values or float
 // pairs).  Shared by ew_lsrk45_step (scratch owned by the context) and
 // ew_lsrk45_step_static (scratch in the static device array).
-// First LSRK45 stage from the FP64 state in vec_n (input and accumulator at
-// once), new accumulator to acc, next stage input to X0.  Compensated
-// Cartesian path: the state is first split in place into float pairs (vec_n
-// is a register of the step), and the stage runs as the middle-stage kernel
-// on them, like the first stage of a later step in a multi-step call; the
-// values are the same exact splits the FP64-input kernel forms on load, at
-// 0.6 of its cost.  Otherwise the FP64-input kernel.
-int ff_first_stage(ew_ctx* ctx, double* vec_n, double* acc, float* X0, double f1, double f2) {
-  using namespace ew;
-  if (ctx->ff && ctx->line) {
-    const cudaError_t e = launch_split_pairs(vec_n, ctx->n_dofs, vec_n, ctx->stream);
-    ++ctx->launches;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "split to float pairs");
-    return launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, vec_n, vec_n, X0, acc, MODE_RK_MID, f1, f2,
-                        1.0f);
-  }
-  return launch_stage(ctx, STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, acc, MODE_RK_MID, f1, f2, 1.0f);
-}
+// One stage of the LSRK45 schedule: the arguments of its launch.
+struct StageCall {
+  int variant, cvar;
+  const double* A;
+  const void* X;
+  void* Xout;
+  double* Aout;
+  int mode;
+  double f1, f2;
+};
 
-int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double* T, float* X0,
-                  float* X1) {
+// The five stages of one LowStorageRK45Reg2 step (time_integrators.cc:235-283)
+// on the registers vec_n (the state in; then a register), vec_np (the new
+// state), T (FP64 scratch) and X0, X1 (stage inputs of the reduced-precision
+// paths).  *split: the compensated Cartesian path first splits the FP64
+// state in vec_n in place into float pairs, and its first stage runs as the
+// middle-stage kernel on them, like the first stage of a later step in a
+// multi-step call (the same exact splits the FP64-input kernel forms on
+// load, at 0.6 of its cost).
+void lsrk45_plan(const ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double* T, float* X0,
+                 float* X1, StageCall st[5], bool* split) {
   using namespace ew;
-  int rc;
   const double f1[5] = {kA21 * dt, kA32 * dt, kA43 * dt, kA54 * dt, kB5 * dt};
   const double f2[5] = {(kB1 - kA21) * dt, (kB2 - kA32) * dt, (kB3 - kA43) * dt, (kB4 - kA54) * dt,
                         0.0};
+  *split = false;
   if (!ctx->mixed) {
     // Three FP64 registers N = vec_n, P = vec_np, T = scratch.  The stage
     // input is read by neighbouring cells, so the new accumulator goes to
@@ -1288,29 +1304,49 @@ int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double*
     // the old accumulator in place (cell-local).
     double* N = vec_n;
     double* P = vec_np;
-    struct S {
-      const double* X;
-      const double* A;
-      double* Xo;
-      double* Ao;
-    } st[5] = {{N, N, T, P}, {T, P, P, N}, {P, N, N, T}, {N, T, T, P}, {T, P, nullptr, P}};
-    for (int s = 0; s < 5; ++s) {
-      rc = launch_stage(ctx, STAGE_F64, s < 4 ? CV_F64_MID : CV_F64_LAST, st[s].A, st[s].X,
-                        st[s].Xo, st[s].Ao, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
-      if (rc) return rc;
-    }
-    return EW_OK;
+    const double* X[5] = {N, T, P, N, T};
+    const double* A[5] = {N, P, N, T, P};
+    double* Xo[5] = {T, P, N, T, nullptr};
+    double* Ao[5] = {P, N, T, P, P};
+    for (int s = 0; s < 5; ++s)
+      st[s] = StageCall{STAGE_F64, s < 4 ? CV_F64_MID : CV_F64_LAST, A[s], X[s], Xo[s], Ao[s],
+                        s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s]};
+    return;
   }
   // mixed: accumulator in vec_np (in place; on Cartesian meshes a float-float
   // pair between the stages, FP64 at the end), FP32 stage inputs ping-pong
-  if ((rc = ff_first_stage(ctx, vec_n, vec_np, X0, f1[0], f2[0]))) return rc;
+  if (ctx->ff && ctx->line) {
+    *split = true;
+    st[0] = StageCall{STAGE_MIX_IN32, CV_MIX_MID, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0], f2[0]};
+  } else {
+    st[0] = StageCall{STAGE_MIX_IN64, CV_MIX_S1, vec_n, vec_n, X0, vec_np, MODE_RK_MID, f1[0], f2[0]};
+  }
   const float* xin[4] = {X0, X1, X0, X1};
   float* xout[4] = {X1, X0, X1, nullptr};
-  for (int s = 1; s < 5; ++s) {
-    rc = launch_stage(ctx, STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1],
-                      xout[s - 1], vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s], 1.0f);
-    if (rc) return rc;
-  }
+  for (int s = 1; s < 5; ++s)
+    st[s] = StageCall{STAGE_MIX_IN32, s < 4 ? CV_MIX_MID : CV_MIX_LAST, vec_np, xin[s - 1], xout[s - 1],
+                      vec_np, s < 4 ? MODE_RK_MID : MODE_RK_LAST, f1[s], f2[s]};
+}
+
+int run_stage(ew_ctx* ctx, const StageCall& s) {
+  return launch_stage(ctx, s.variant, s.cvar, s.A, s.X, s.Xout, s.Aout, s.mode, s.f1, s.f2, 1.0f);
+}
+
+int split_state(ew_ctx* ctx, double* v, int64_t n, cudaStream_t stream) {
+  const cudaError_t e = ew::launch_split_pairs(v, n, v, stream);
+  ++ctx->launches;
+  return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "split to float pairs");
+}
+
+int lsrk45_stages(ew_ctx* ctx, double dt, double* vec_n, double* vec_np, double* T, float* X0,
+                  float* X1) {
+  StageCall st[5];
+  bool split = false;
+  lsrk45_plan(ctx, dt, vec_n, vec_np, T, X0, X1, st, &split);
+  int rc;
+  if (split && (rc = split_state(ctx, vec_n, ctx->n_dofs, ctx->stream))) return rc;
+  for (int s = 0; s < 5; ++s)
+    if ((rc = run_stage(ctx, st[s]))) return rc;
   return EW_OK;
 }
 }  // namespace
@@ -1322,6 +1358,64 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np) {
     return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step: vec_n and vec_np must be distinct");
   return lsrk45_stages(ctx, dt, vec_n, vec_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1]);
 }
+
+namespace {
+int host_chunk_plan(ew_ctx* c) {
+  if (!c->hchunks.empty()) return EW_OK;
+  const int64_t cellsz = (int64_t)c->F * c->N;
+  if (c->line) {
+    const int K = std::max(1, std::min<int>(kHostChunks, c->n_work_cart));
+    const int per = (c->n_work_cart + K - 1) / K;
+    const int nf = 2 * c->dim;
+    std::vector<int32_t> nbr((size_t)c->n_cells * nf);
+    const cudaError_t e =
+        cudaMemcpy(nbr.data(), c->d_nbr, nbr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "neighbour table readback");
+    for (int k = 0; k < K; ++k) {
+      ew_ctx::HostChunk h;
+      h.item_begin = k * per;
+      h.n_items = std::min(per, c->n_work_cart - k * per);
+      if (h.n_items <= 0) break;
+      const int64_t cb = (int64_t)h.item_begin * c->cb_cart;
+      const int64_t ce = std::min<int64_t>((int64_t)(h.item_begin + h.n_items) * c->cb_cart, c->n_cells);
+      h.dof_begin = cb * cellsz;
+      h.n_dofs = (ce - cb) * cellsz;
+      h.lo = h.hi = k;
+      for (int64_t cell = cb; cell < ce; ++cell)
+        for (int f = 0; f < nf; ++f) {
+          const int32_t nb = nbr[(size_t)cell * nf + f];
+          if (nb < 0) continue;
+          const int kc = (int)std::min<int64_t>(((int64_t)nb / c->cb_cart) / per, K - 1);
+          h.lo = std::min(h.lo, kc);
+          h.hi = std::max(h.hi, kc);
+        }
+      c->hchunks.push_back(h);
+    }
+  } else {
+    const int64_t n = c->n_dofs, chunk = (n + kHostChunks - 1) / kHostChunks;
+    for (int k = 0; k < kHostChunks && k * chunk < n; ++k) {
+      ew_ctx::HostChunk h;
+      h.dof_begin = k * chunk;
+      h.n_dofs = std::min(chunk, n - k * chunk);
+      c->hchunks.push_back(h);
+    }
+  }
+  return EW_OK;
+}
+
+// line kernel launches of a scope over one work-item range
+struct WorkRange {
+  ew_ctx* c;
+  WorkRange(ew_ctx* ctx, int begin, int count) : c(ctx) {
+    c->wr_begin = begin;
+    c->wr_count = count;
+  }
+  ~WorkRange() {
+    c->wr_begin = 0;
+    c->wr_count = -1;
+  }
+};
+}  // namespace
 
 int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h_vec_np) {
   int rc = check(ctx);
@@ -1339,52 +1433,90 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
         (e = cudaEventCreateWithFlags(&ctx->ev_h2d, fl)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_step, fl)) != cudaSuccess)
       return cuda_fail(ctx, e, "host step streams");
-    for (cudaEvent_t& ev : ctx->ev_d2h)
-      if ((e = cudaEventCreateWithFlags(&ev, fl)) != cudaSuccess) return cuda_fail(ctx, e, "host step events");
+    for (int k = 0; k < kHostChunks; ++k)
+      if ((e = cudaEventCreateWithFlags(&ctx->ev_d2h[k], fl)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&ctx->ev_in[k], fl)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&ctx->ev_s5[k], fl)) != cudaSuccess)
+        return cuda_fail(ctx, e, "host step events");
   }
+  if ((rc = host_chunk_plan(ctx))) return rc;
+  const int K = (int)ctx->hchunks.size();
   double* d_n = ctx->d_hstate[0];
   double* d_np = ctx->d_hstate[1];
-  const int64_t n = ctx->n_dofs;
-  const int64_t chunk = (n + kHostChunks - 1) / kHostChunks;
+  StageCall st[5];
+  bool split = false;
+  lsrk45_plan(ctx, dt, d_n, d_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1], st, &split);
+  // With the line kernel the first and the last stage run chunk by chunk:
+  // each chunk of the first stage starts once the input chunks its cells'
+  // neighbours lie in have arrived (and are split), and each chunk's copy
+  // to the host starts once the last stage has finished that chunk.  The
+  // middle stages run whole.
+  const bool staged = ctx->line;
   // the input chunks that the previous call's output copies are still writing
   const bool chained = ctx->d2h_pending && h_vec_n == ctx->last_host_out;
+  auto ordering = [&](cudaError_t err) { return cuda_fail(ctx, err, "host step ordering"); };
   // host -> device, after the work already on the context stream (the
-  // previous step used d_n as a register) and, chunk by chunk, after the
-  // previous call's copy of the same chunk to the host
+  // previous step's use of d_n) and, chunk by chunk, after the previous
+  // call's copy of the same chunk to the host; any other input may still
+  // overlap the previous output: after all of it
   if ((e = cudaEventRecord(ctx->ev_entry, ctx->stream)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_entry, 0)) != cudaSuccess)
-    return cuda_fail(ctx, e, "host step ordering");
-  // any other input may still overlap the previous output: after all of it
-  if (ctx->d2h_pending && !chained &&
-      (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[kHostChunks - 1], 0)) != cudaSuccess)
-    return cuda_fail(ctx, e, "host step ordering");
-  for (int k = 0; k < kHostChunks; ++k) {
-    const int64_t o = k * chunk, m = std::min(chunk, n - o);
-    if (m <= 0) break;
-    if (chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[k], 0)) != cudaSuccess)
-      return cuda_fail(ctx, e, "host step ordering");
-    if ((e = cudaMemcpyAsync(d_n + o, h_vec_n + o, (size_t)m * sizeof(double), cudaMemcpyHostToDevice,
-                             ctx->s_h2d)) != cudaSuccess)
+    return ordering(e);
+  if (ctx->d2h_pending && !chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[K - 1], 0)) != cudaSuccess)
+    return ordering(e);
+  for (int k = 0; k < K; ++k) {
+    const ew_ctx::HostChunk& h = ctx->hchunks[k];
+    if (chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[k], 0)) != cudaSuccess) return ordering(e);
+    if ((e = cudaMemcpyAsync(d_n + h.dof_begin, h_vec_n + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
+                             cudaMemcpyHostToDevice, ctx->s_h2d)) != cudaSuccess)
       return cuda_fail(ctx, e, "host to device copy");
+    if (split && (rc = split_state(ctx, d_n + h.dof_begin, h.n_dofs, ctx->s_h2d))) return rc;
+    if ((e = cudaEventRecord(ctx->ev_in[k], ctx->s_h2d)) != cudaSuccess) return ordering(e);
   }
-  // the step: after every input chunk and after the previous call's output
-  // copies (they read d_np, which the step writes)
-  if ((e = cudaEventRecord(ctx->ev_h2d, ctx->s_h2d)) != cudaSuccess ||
-      (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_h2d, 0)) != cudaSuccess ||
-      (ctx->d2h_pending && (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[kHostChunks - 1], 0)) != cudaSuccess))
-    return cuda_fail(ctx, e, "host step ordering");
-  if ((rc = lsrk45_stages(ctx, dt, d_n, d_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1]))) return rc;
-  // device -> host, chunk by chunk, each chunk's completion recorded
-  if ((e = cudaEventRecord(ctx->ev_step, ctx->stream)) != cudaSuccess ||
-      (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_step, 0)) != cudaSuccess)
-    return cuda_fail(ctx, e, "host step ordering");
-  for (int k = 0; k < kHostChunks; ++k) {
-    const int64_t o = k * chunk, m = std::min(chunk, n - o);
-    if (m > 0 && (e = cudaMemcpyAsync(h_vec_np + o, d_np + o, (size_t)m * sizeof(double),
-                                      cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess)
-      return cuda_fail(ctx, e, "device to host copy");
-    if ((e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
-      return cuda_fail(ctx, e, "host step ordering");
+  if (staged) {
+    // first stage, chunk by chunk (it writes d_np, which the previous call's
+    // copies read: ordered through the input chunks above)
+    for (int k = 0; k < K; ++k) {
+      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      for (int j = h.lo; j <= h.hi; ++j)
+        if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_in[j], 0)) != cudaSuccess) return ordering(e);
+      WorkRange wr(ctx, h.item_begin, h.n_items);
+      if ((rc = run_stage(ctx, st[0]))) return rc;
+    }
+    for (int s = 1; s < 4; ++s)
+      if ((rc = run_stage(ctx, st[s]))) return rc;
+    for (int k = 0; k < K; ++k) {
+      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      {
+        WorkRange wr(ctx, h.item_begin, h.n_items);
+        if ((rc = run_stage(ctx, st[4]))) return rc;
+      }
+      if ((e = cudaEventRecord(ctx->ev_s5[k], ctx->stream)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_s5[k], 0)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess ||
+          (e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
+        return cuda_fail(ctx, e, "device to host copy");
+    }
+  } else {
+    // the step after every input chunk and after the previous call's output
+    // copies (they read d_np, which the step writes)
+    if ((e = cudaEventRecord(ctx->ev_h2d, ctx->s_h2d)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_h2d, 0)) != cudaSuccess ||
+        (ctx->d2h_pending && (e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[K - 1], 0)) != cudaSuccess))
+      return ordering(e);
+    for (int s = 0; s < 5; ++s)
+      if ((rc = run_stage(ctx, st[s]))) return rc;
+    if ((e = cudaEventRecord(ctx->ev_step, ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_step, 0)) != cudaSuccess)
+      return ordering(e);
+    for (int k = 0; k < K; ++k) {
+      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      if ((e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess ||
+          (e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
+        return cuda_fail(ctx, e, "device to host copy");
+    }
   }
   ctx->last_host_out = h_vec_np;
   ctx->d2h_pending = true;
@@ -1395,7 +1527,7 @@ int ew_wait_host_copies(ew_ctx* ctx) {
   int rc = check(ctx);
   if (rc) return rc;
   if (!ctx->d2h_pending) return EW_OK;
-  const cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[kHostChunks - 1], 0);
+  const cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev_d2h[ctx->hchunks.size() - 1], 0);
   return e == cudaSuccess ? EW_OK : cuda_fail(ctx, e, "host copy ordering");
 }
 
@@ -1556,9 +1688,12 @@ int ew_lsrk45_steps(ew_ctx* ctx, double dt, int64_t n_steps, double* vec_n, doub
     double* ac = vec_np;  // accumulator of the current step
     for (int64_t step = 0; step < n_steps; ++step) {
       const bool last_step = step + 1 == n_steps;
-      if (step == 0)
-        rc = ff_first_stage(ctx, st, ac, xb[0], f1[0], f2[0]);
-      else
+      if (step == 0) {
+        // the FP64 state split in place into float pairs: then like any step
+        if ((rc = split_state(ctx, st, ctx->n_dofs, ctx->stream))) return rc;
+        rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, st, st, xb[0], ac, MODE_RK_MID, f1[0], f2[0],
+                          1.0f);
+      } else
         rc = launch_stage(ctx, STAGE_MIX_IN32, CV_MIX_MID, st, st, xb[0], ac, MODE_RK_MID, f1[0],
                           f2[0], 1.0f);
       if (rc) return rc;
