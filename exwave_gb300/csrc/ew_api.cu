@@ -616,6 +616,9 @@ struct ew_ctx {
     int lo = 0, hi = 0;
   };
   std::vector<HostChunk> hchunks;
+  // every chunk's neighbours lie in the chunk itself or the two next to it:
+  // all five stages can run chunk by chunk as a wavefront
+  bool host_wave = false;
   const double* last_host_out = nullptr;  // host output of the previous host step
   bool d2h_pending = false;
   std::string last_error;
@@ -1391,6 +1394,9 @@ int host_chunk_plan(ew_ctx* c) {
         }
       c->hchunks.push_back(h);
     }
+    c->host_wave = true;
+    for (int k = 0; k < (int)c->hchunks.size(); ++k)
+      if (c->hchunks[k].lo < k - 1 || c->hchunks[k].hi > k + 1) c->host_wave = false;
   } else {
     const int64_t n = c->n_dofs, chunk = (n + kHostChunks - 1) / kHostChunks;
     for (int k = 0; k < kHostChunks && k * chunk < n; ++k) {
@@ -1473,7 +1479,40 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     if (split && (rc = split_state(ctx, d_n + h.dof_begin, h.n_dofs, ctx->s_h2d))) return rc;
     if ((e = cudaEventRecord(ctx->ev_in[k], ctx->s_h2d)) != cudaSuccess) return ordering(e);
   }
-  if (staged) {
+  // copy of chunk k to the host once the last stage has finished it
+  auto copy_out = [&](int k) -> int {
+    const ew_ctx::HostChunk& h = ctx->hchunks[k];
+    if ((e = cudaEventRecord(ctx->ev_s5[k], ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_s5[k], 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess ||
+        (e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
+      return cuda_fail(ctx, e, "device to host copy");
+    return EW_OK;
+  };
+  if (staged && ctx->host_wave) {
+    // Wavefront: stage s of chunk k is launched on diagonal d = k + 2 s.
+    // It reads the previous stage's output on chunks k-1..k+1 (diagonals
+    // k + 2 s - 1 and earlier) and overwrites registers that the previous
+    // stage read on those chunks, so every dependence points to an earlier
+    // diagonal, and the single compute stream runs them in order.  Within a
+    // diagonal the first stage, which waits for its input chunks, comes
+    // last, so ready work is never queued behind that wait.
+    for (int d = 0; d < K + 8; ++d)
+      for (int s = 4; s >= 0; --s) {
+        const int k = d - 2 * s;
+        if (k < 0 || k >= K) continue;
+        const ew_ctx::HostChunk& h = ctx->hchunks[k];
+        if (s == 0)
+          for (int j = h.lo; j <= h.hi; ++j)
+            if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_in[j], 0)) != cudaSuccess) return ordering(e);
+        {
+          WorkRange wr(ctx, h.item_begin, h.n_items);
+          if ((rc = run_stage(ctx, st[s]))) return rc;
+        }
+        if (s == 4 && (rc = copy_out(k))) return rc;
+      }
+  } else if (staged) {
     // first stage, chunk by chunk (it writes d_np, which the previous call's
     // copies read: ordered through the input chunks above)
     for (int k = 0; k < K; ++k) {
@@ -1491,12 +1530,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
         WorkRange wr(ctx, h.item_begin, h.n_items);
         if ((rc = run_stage(ctx, st[4]))) return rc;
       }
-      if ((e = cudaEventRecord(ctx->ev_s5[k], ctx->stream)) != cudaSuccess ||
-          (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_s5[k], 0)) != cudaSuccess ||
-          (e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
-                               cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess ||
-          (e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
-        return cuda_fail(ctx, e, "device to host copy");
+      if ((rc = copy_out(k))) return rc;
     }
   } else {
     // the step after every input chunk and after the previous call's output

@@ -2,7 +2,10 @@
 integrator's storage) equals the device step bit for bit, whether the host
 array is stepped in place (each call's copy in chained to the previous
 call's copy out, chunk by chunk), ping-ponged between two arrays, or not
-pinned; ew_wait_host_copies orders the context stream after the copies."""
+pinned, and whichever chunk schedule the mesh allows (curved cells: the
+whole step between the copies; axis-aligned: the first and last stage by
+chunks, or all five stages as a wavefront over the chunks);
+ew_wait_host_copies orders the context stream after the copies."""
 import numpy as np
 import pytest
 
@@ -30,11 +33,14 @@ def _device_steps(op, dt, u0, n, torch):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_ff"])
-@pytest.mark.parametrize("dim,k,n", [(3, 3, 5), (2, 5, 7), (3, 2, 3)])
-def test_host_step_equals_device_step(ew_torch, precision, dim, k, n):
+# small meshes (neighbours several chunks apart: first and last stage by
+# chunks) and meshes whose chunks hold more than one layer of cells (every
+# neighbour in the same or the next chunk: all stages as a wavefront)
+@pytest.mark.parametrize("dim,k,n,f", [(3, 3, 5, 0.0), (2, 5, 7, 0.05), (3, 2, 3, 0.0), (3, 2, 16, 0.0),
+                                       (2, 3, 20, 0.0)])
+def test_host_step_equals_device_step(ew_torch, precision, dim, k, n, f):
     ew, torch = ew_torch
-    m = ew.hypercube(dim, n, 0, 0.05 if dim == 2 else 0.0,
-                     boundary_ids=[1, 2, 3, 1] if dim == 2 else [1, 2, 3, 1, 2, 3])
+    m = ew.hypercube(dim, n, 0, f, boundary_ids=[1, 2, 3, 1] if dim == 2 else [1, 2, 3, 1, 2, 3])
     rng = np.random.default_rng(dim * 10 + k)
     m.speed = rng.uniform(1.0, 3.0, m.n_cells)
     m.density = rng.uniform(1.0, 2.0, m.n_cells)
