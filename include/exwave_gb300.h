@@ -137,8 +137,9 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
  * input is the previous call's output, each chunk's host-to-device copy
  * starts as soon as the previous call's device-to-host copy of that chunk
  * has landed, so the two directions overlap; on axis-aligned meshes the
- * first and last stages also run chunk by chunk, beside the copies.  Results
- * equal ew_lsrk45_step's bit for bit.  Host arrays should be pinned
+ * stages also run chunk by chunk beside the copies (all five as a wavefront
+ * when every chunk's neighbours lie in the chunks next to it, else the
+ * first and the last).  Results equal ew_lsrk45_step's bit for bit.  Host arrays should be pinned
  * (cudaHostAlloc / cudaHostRegister) for the copies to be asynchronous.
  * Returns once the work is enqueued; h_vec_np is complete after
  * ew_synchronize, or on the context stream after ew_wait_host_copies. */
