@@ -2,7 +2,7 @@
 
 The reference knows one material and the membrane initial field
 (input_parameters.cc:22-29, input_parameters.h:95-128); the Gaussian
-pressure pulse and the two-layer medium are this build's own inputs, so they
+pressure pulse and the two-layer medium have no counterpart there, so they
 are checked here against their definitions:
 - the oracle's Gaussian projection is the pulse sampled at the Gauss points
   (the collocation form of project_initial_field,
