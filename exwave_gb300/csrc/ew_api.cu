@@ -15,6 +15,7 @@
 
 #include "../../include/exwave_gb300.h"
 #include "ew_basis.h"
+#include "ew_hostplan.h"
 #include "ew_ff.cuh"
 #include "ew_internal.h"
 #include "ew_launch.h"
@@ -610,12 +611,7 @@ struct ew_ctx {
   // the chunks: with the line kernel, runs of whole work items, and the
   // input chunks that hold their cells' neighbours (lo..hi); else equal
   // runs of DoFs
-  struct HostChunk {
-    int item_begin = 0, n_items = 0;
-    int64_t dof_begin = 0, n_dofs = 0;
-    int lo = 0, hi = 0;
-  };
-  std::vector<HostChunk> hchunks;
+  std::vector<ew::HostChunk> hchunks;
   // every chunk's neighbours lie in the chunk itself or the two next to it:
   // all five stages can run chunk by chunk as a wavefront
   bool host_wave = false;
@@ -1367,40 +1363,17 @@ int host_chunk_plan(ew_ctx* c) {
   if (!c->hchunks.empty()) return EW_OK;
   const int64_t cellsz = (int64_t)c->F * c->N;
   if (c->line) {
-    const int K = std::max(1, std::min<int>(kHostChunks, c->n_work_cart));
-    const int per = (c->n_work_cart + K - 1) / K;
     const int nf = 2 * c->dim;
     std::vector<int32_t> nbr((size_t)c->n_cells * nf);
     const cudaError_t e =
         cudaMemcpy(nbr.data(), c->d_nbr, nbr.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, "neighbour table readback");
-    for (int k = 0; k < K; ++k) {
-      ew_ctx::HostChunk h;
-      h.item_begin = k * per;
-      h.n_items = std::min(per, c->n_work_cart - k * per);
-      if (h.n_items <= 0) break;
-      const int64_t cb = (int64_t)h.item_begin * c->cb_cart;
-      const int64_t ce = std::min<int64_t>((int64_t)(h.item_begin + h.n_items) * c->cb_cart, c->n_cells);
-      h.dof_begin = cb * cellsz;
-      h.n_dofs = (ce - cb) * cellsz;
-      h.lo = h.hi = k;
-      for (int64_t cell = cb; cell < ce; ++cell)
-        for (int f = 0; f < nf; ++f) {
-          const int32_t nb = nbr[(size_t)cell * nf + f];
-          if (nb < 0) continue;
-          const int kc = (int)std::min<int64_t>(((int64_t)nb / c->cb_cart) / per, K - 1);
-          h.lo = std::min(h.lo, kc);
-          h.hi = std::max(h.hi, kc);
-        }
-      c->hchunks.push_back(h);
-    }
-    c->host_wave = true;
-    for (int k = 0; k < (int)c->hchunks.size(); ++k)
-      if (c->hchunks[k].lo < k - 1 || c->hchunks[k].hi > k + 1) c->host_wave = false;
+    c->host_wave = ew::host_chunk_plan_items(c->n_work_cart, c->cb_cart, c->n_cells, cellsz, nf, nbr.data(),
+                                             kHostChunks, &c->hchunks);
   } else {
     const int64_t n = c->n_dofs, chunk = (n + kHostChunks - 1) / kHostChunks;
     for (int k = 0; k < kHostChunks && k * chunk < n; ++k) {
-      ew_ctx::HostChunk h;
+      ew::HostChunk h;
       h.dof_begin = k * chunk;
       h.n_dofs = std::min(chunk, n - k * chunk);
       c->hchunks.push_back(h);
@@ -1471,7 +1444,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
   if (ctx->d2h_pending && !chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[K - 1], 0)) != cudaSuccess)
     return ordering(e);
   for (int k = 0; k < K; ++k) {
-    const ew_ctx::HostChunk& h = ctx->hchunks[k];
+    const ew::HostChunk& h = ctx->hchunks[k];
     if (chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[k], 0)) != cudaSuccess) return ordering(e);
     if ((e = cudaMemcpyAsync(d_n + h.dof_begin, h_vec_n + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
                              cudaMemcpyHostToDevice, ctx->s_h2d)) != cudaSuccess)
@@ -1481,7 +1454,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
   }
   // copy of chunk k to the host once the last stage has finished it
   auto copy_out = [&](int k) -> int {
-    const ew_ctx::HostChunk& h = ctx->hchunks[k];
+    const ew::HostChunk& h = ctx->hchunks[k];
     if ((e = cudaEventRecord(ctx->ev_s5[k], ctx->stream)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_s5[k], 0)) != cudaSuccess ||
         (e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
@@ -1502,7 +1475,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
       for (int s = 4; s >= 0; --s) {
         const int k = d - 2 * s;
         if (k < 0 || k >= K) continue;
-        const ew_ctx::HostChunk& h = ctx->hchunks[k];
+        const ew::HostChunk& h = ctx->hchunks[k];
         if (s == 0)
           for (int j = h.lo; j <= h.hi; ++j)
             if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_in[j], 0)) != cudaSuccess) return ordering(e);
@@ -1516,7 +1489,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     // first stage, chunk by chunk (it writes d_np, which the previous call's
     // copies read: ordered through the input chunks above)
     for (int k = 0; k < K; ++k) {
-      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      const ew::HostChunk& h = ctx->hchunks[k];
       for (int j = h.lo; j <= h.hi; ++j)
         if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_in[j], 0)) != cudaSuccess) return ordering(e);
       WorkRange wr(ctx, h.item_begin, h.n_items);
@@ -1525,7 +1498,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     for (int s = 1; s < 4; ++s)
       if ((rc = run_stage(ctx, st[s]))) return rc;
     for (int k = 0; k < K; ++k) {
-      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      const ew::HostChunk& h = ctx->hchunks[k];
       {
         WorkRange wr(ctx, h.item_begin, h.n_items);
         if ((rc = run_stage(ctx, st[4]))) return rc;
@@ -1545,7 +1518,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
         (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_step, 0)) != cudaSuccess)
       return ordering(e);
     for (int k = 0; k < K; ++k) {
-      const ew_ctx::HostChunk& h = ctx->hchunks[k];
+      const ew::HostChunk& h = ctx->hchunks[k];
       if ((e = cudaMemcpyAsync(h_vec_np + h.dof_begin, d_np + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
                                cudaMemcpyDeviceToHost, ctx->s_d2h)) != cudaSuccess ||
           (e = cudaEventRecord(ctx->ev_d2h[k], ctx->s_d2h)) != cudaSuccess)
