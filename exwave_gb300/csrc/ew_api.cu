@@ -1425,11 +1425,14 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
   StageCall st[5];
   bool split = false;
   lsrk45_plan(ctx, dt, d_n, d_np, ctx->d_tmp64, ctx->d_x32[0], ctx->d_x32[1], st, &split);
-  // With the line kernel the first and the last stage run chunk by chunk:
-  // each chunk of the first stage starts once the input chunks its cells'
-  // neighbours lie in have arrived (and are split), and each chunk's copy
-  // to the host starts once the last stage has finished that chunk.  The
-  // middle stages run whole.
+  // With the line kernel the stages run chunk by chunk: each chunk of the
+  // first stage starts once the input chunks its cells' neighbours lie in
+  // have arrived (and are split), and each chunk's copy to the host starts
+  // once the last stage has finished that chunk.  The middle stages run as
+  // a wavefront over the chunks where every chunk's neighbours lie in the
+  // chunks next to it (host_wave), else whole.  The first stage is always
+  // the first launch to touch a chunk, after that chunk's input (and so
+  // after the previous call's copy out of it, which reads d_np).
   const bool staged = ctx->line;
   // the input chunks that the previous call's output copies are still writing
   const bool chained = ctx->d2h_pending && h_vec_n == ctx->last_host_out;
