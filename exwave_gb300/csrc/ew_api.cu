@@ -606,6 +606,15 @@ struct ew_ctx {
   cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
   cudaEvent_t ev_entry = nullptr, ev_h2d = nullptr, ev_step = nullptr;
   cudaEvent_t ev_d2h[kHostChunks] = {};
+  // the host step's compute runs on its own stream: ev_comp marks its end
+  // (every other entry point orders the context stream after it), and
+  // ev_nfree[k] the point after which the step no longer touches chunk k of
+  // the device state d_hstate[0], so that the next call's copy in of that
+  // chunk may start
+  cudaStream_t s_comp = nullptr;
+  cudaEvent_t ev_comp = nullptr;
+  cudaEvent_t ev_nfree[kHostChunks] = {};
+  bool comp_pending = false, nfree_valid = false;
   cudaEvent_t ev_in[kHostChunks] = {};  // input chunk on the device (and split)
   cudaEvent_t ev_s5[kHostChunks] = {};  // last stage done on the chunk
   // the chunks: with the line kernel, runs of whole work items, and the
@@ -658,6 +667,7 @@ void free_ctx(ew_ctx* c) {
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
+  if (c->s_comp) cudaStreamSynchronize(c->s_comp);
   if (c->s_d2h) cudaStreamSynchronize(c->s_d2h);
   if (c->s_h2d) cudaStreamSynchronize(c->s_h2d);
   void* ptrs[] = {c->d_nbr, c->d_geo, c->d_mat, c->d_verts, c->d_basis, c->d_nodes,
@@ -666,14 +676,15 @@ void free_ctx(ew_ctx* c) {
                   c->d_hstate[0], c->d_hstate[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  cudaEvent_t evs[] = {c->ev_entry, c->ev_h2d, c->ev_step};
+  cudaEvent_t evs[] = {c->ev_entry, c->ev_h2d, c->ev_step, c->ev_comp};
   for (cudaEvent_t e : evs)
     if (e) cudaEventDestroy(e);
   for (int k = 0; k < kHostChunks; ++k)
-    for (cudaEvent_t e : {c->ev_d2h[k], c->ev_in[k], c->ev_s5[k]})
+    for (cudaEvent_t e : {c->ev_d2h[k], c->ev_in[k], c->ev_s5[k], c->ev_nfree[k]})
       if (e) cudaEventDestroy(e);
   if (c->s_h2d) cudaStreamDestroy(c->s_h2d);
   if (c->s_d2h) cudaStreamDestroy(c->s_d2h);
+  if (c->s_comp) cudaStreamDestroy(c->s_comp);
   cudaSetDevice(prev);
   delete c;
 }
@@ -772,10 +783,24 @@ int default_cb(int points, int requested) {
   return std::max(1, 512 / points);
 }
 
-int check(ew_ctx* c) {
+int set_device(ew_ctx* c) {
   if (!c) return EW_ERR_INVALID;
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  return EW_OK;
+}
+
+// Entry of every operation on the context stream: after the device and, if
+// a host step's compute is still running on its own stream, after it (the
+// two share the context's scratch vectors).
+int check(ew_ctx* c) {
+  int rc = set_device(c);
+  if (rc) return rc;
+  if (c->comp_pending) {
+    const cudaError_t e = cudaStreamWaitEvent(c->stream, c->ev_comp, 0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "host step ordering");
+    c->comp_pending = false;
+  }
   return EW_OK;
 }
 
@@ -1397,7 +1422,9 @@ struct WorkRange {
 }  // namespace
 
 int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h_vec_np) {
-  int rc = check(ctx);
+  // the previous host step's compute is not waited for here: only what it
+  // touches is (below)
+  int rc = set_device(ctx);
   if (rc) return rc;
   if (!h_vec_n || !h_vec_np) return fail(ctx, EW_ERR_INVALID, "ew_lsrk45_step_host: NULL host vector");
   cudaError_t e = cudaSuccess;
@@ -1408,6 +1435,8 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     const unsigned fl = cudaEventDisableTiming;
     if ((e = cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->s_comp, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_comp, fl)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_entry, fl)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_h2d, fl)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_step, fl)) != cudaSuccess)
@@ -1415,7 +1444,8 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     for (int k = 0; k < kHostChunks; ++k)
       if ((e = cudaEventCreateWithFlags(&ctx->ev_d2h[k], fl)) != cudaSuccess ||
           (e = cudaEventCreateWithFlags(&ctx->ev_in[k], fl)) != cudaSuccess ||
-          (e = cudaEventCreateWithFlags(&ctx->ev_s5[k], fl)) != cudaSuccess)
+          (e = cudaEventCreateWithFlags(&ctx->ev_s5[k], fl)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&ctx->ev_nfree[k], fl)) != cudaSuccess)
         return cuda_fail(ctx, e, "host step events");
   }
   if ((rc = host_chunk_plan(ctx))) return rc;
@@ -1438,16 +1468,21 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
   const bool chained = ctx->d2h_pending && h_vec_n == ctx->last_host_out;
   auto ordering = [&](cudaError_t err) { return cuda_fail(ctx, err, "host step ordering"); };
   // host -> device, after the work already on the context stream (the
-  // previous step's use of d_n) and, chunk by chunk, after the previous
-  // call's copy of the same chunk to the host; any other input may still
-  // overlap the previous output: after all of it
+  // caller's, and other operations of the context) and, chunk by chunk,
+  // after the previous host step has released that chunk of d_n and copied
+  // the same chunk to the host; any other input may still overlap the
+  // previous output: after all of it.  The compute, on its own stream, also
+  // follows the context stream's work.
   if ((e = cudaEventRecord(ctx->ev_entry, ctx->stream)) != cudaSuccess ||
-      (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_entry, 0)) != cudaSuccess)
+      (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_entry, 0)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(ctx->s_comp, ctx->ev_entry, 0)) != cudaSuccess)
     return ordering(e);
   if (ctx->d2h_pending && !chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[K - 1], 0)) != cudaSuccess)
     return ordering(e);
   for (int k = 0; k < K; ++k) {
     const ew::HostChunk& h = ctx->hchunks[k];
+    if (ctx->nfree_valid && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_nfree[k], 0)) != cudaSuccess)
+      return ordering(e);
     if (chained && (e = cudaStreamWaitEvent(ctx->s_h2d, ctx->ev_d2h[k], 0)) != cudaSuccess) return ordering(e);
     if ((e = cudaMemcpyAsync(d_n + h.dof_begin, h_vec_n + h.dof_begin, (size_t)h.n_dofs * sizeof(double),
                              cudaMemcpyHostToDevice, ctx->s_h2d)) != cudaSuccess)
@@ -1455,6 +1490,24 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
     if (split && (rc = split_state(ctx, d_n + h.dof_begin, h.n_dofs, ctx->s_h2d))) return rc;
     if ((e = cudaEventRecord(ctx->ev_in[k], ctx->s_h2d)) != cudaSuccess) return ordering(e);
   }
+  // The compute runs on s_comp (the launches go to ctx->stream, swapped for
+  // this call).  The last stage that touches d_n (as input, accumulator or
+  // output) releases its chunks: chunk k once that stage is done on chunks
+  // k-1..k+1 (wavefront), else once it is done everywhere.
+  struct StreamSwap {
+    ew_ctx* c;
+    cudaStream_t saved;
+    StreamSwap(ew_ctx* ctx) : c(ctx), saved(ctx->stream) { c->stream = c->s_comp; }
+    ~StreamSwap() { c->stream = saved; }
+  } swap(ctx);
+  int last_n = 0;
+  for (int s = 0; s < 5; ++s)
+    if (st[s].X == d_n || st[s].A == d_n || st[s].Xout == d_n || st[s].Aout == d_n) last_n = s;
+  auto release_all = [&]() -> int {
+    for (int k = 0; k < K; ++k)
+      if ((e = cudaEventRecord(ctx->ev_nfree[k], ctx->stream)) != cudaSuccess) return ordering(e);
+    return EW_OK;
+  };
   // copy of chunk k to the host once the last stage has finished it
   auto copy_out = [&](int k) -> int {
     const ew::HostChunk& h = ctx->hchunks[k];
@@ -1486,6 +1539,14 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
           WorkRange wr(ctx, h.item_begin, h.n_items);
           if ((rc = run_stage(ctx, st[s]))) return rc;
         }
+        if (s == last_n) {
+          // chunk k - 1 is released (its readers are chunks k-2..k), and
+          // with the last chunk the last one too
+          if (k >= 1 && (e = cudaEventRecord(ctx->ev_nfree[k - 1], ctx->stream)) != cudaSuccess)
+            return ordering(e);
+          if (k == K - 1 && (e = cudaEventRecord(ctx->ev_nfree[k], ctx->stream)) != cudaSuccess)
+            return ordering(e);
+        }
         if (s == 4 && (rc = copy_out(k))) return rc;
       }
   } else if (staged) {
@@ -1498,8 +1559,11 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
       WorkRange wr(ctx, h.item_begin, h.n_items);
       if ((rc = run_stage(ctx, st[0]))) return rc;
     }
-    for (int s = 1; s < 4; ++s)
+    if (last_n == 0 && (rc = release_all())) return rc;
+    for (int s = 1; s < 4; ++s) {
       if ((rc = run_stage(ctx, st[s]))) return rc;
+      if (s == last_n && (rc = release_all())) return rc;
+    }
     for (int k = 0; k < K; ++k) {
       const ew::HostChunk& h = ctx->hchunks[k];
       {
@@ -1508,6 +1572,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
       }
       if ((rc = copy_out(k))) return rc;
     }
+    if (last_n == 4 && (rc = release_all())) return rc;
   } else {
     // the step after every input chunk and after the previous call's output
     // copies (they read d_np, which the step writes)
@@ -1517,6 +1582,7 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
       return ordering(e);
     for (int s = 0; s < 5; ++s)
       if ((rc = run_stage(ctx, st[s]))) return rc;
+    if ((rc = release_all())) return rc;
     if ((e = cudaEventRecord(ctx->ev_step, ctx->stream)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(ctx->s_d2h, ctx->ev_step, 0)) != cudaSuccess)
       return ordering(e);
@@ -1528,6 +1594,9 @@ int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h
         return cuda_fail(ctx, e, "device to host copy");
     }
   }
+  if ((e = cudaEventRecord(ctx->ev_comp, ctx->stream)) != cudaSuccess) return ordering(e);
+  ctx->comp_pending = true;
+  ctx->nfree_valid = true;
   ctx->last_host_out = h_vec_np;
   ctx->d2h_pending = true;
   return EW_OK;
