@@ -142,7 +142,10 @@ int ew_lsrk45_step(ew_ctx* ctx, double dt, double* vec_n, double* vec_np);
  * first and the last).  Results equal ew_lsrk45_step's bit for bit.  Host arrays should be pinned
  * (cudaHostAlloc / cudaHostRegister) for the copies to be asynchronous.
  * Returns once the work is enqueued; h_vec_np is complete after
- * ew_synchronize, or on the context stream after ew_wait_host_copies. */
+ * ew_synchronize, or on the context stream after ew_wait_host_copies.  The
+ * step itself runs on a stream of the context's own, after the work on the
+ * context stream at the call; every later call on the context orders the
+ * context stream after it. */
 int ew_lsrk45_step_host(ew_ctx* ctx, double dt, const double* h_vec_n, double* h_vec_np);
 /* Orders the context stream after the device-to-host copies of the last
  * ew_lsrk45_step_host call (an event recorded or a synchronize on the stream
