@@ -82,11 +82,6 @@ class Arena {
     }
   }
   size_t free_bytes() const { return size_ - used_; }
-  size_t largest_free() const {
-    size_t m = 0;
-    for (auto& f : free_) m = std::max(m, f.second);
-    return m;
-  }
 
  private:
   size_t size_ = 0, used_ = 0;
